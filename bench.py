@@ -1,0 +1,519 @@
+#!/usr/bin/env python
+"""Benchmark of the labelled-reduction + fill workload on GB300.
+
+Workload (numbagg's grouped / fill hot path): float64 values of shape
+64 x 16,777,216, N(0,1) with 5% NaN; int32 labels along the last axis, uniform in
+[0, K) for K in {16, 4096, 1,000,000}; group_nansum / nanmean / nanvar / nancount /
+nanargmax for each K; ffill / bfill with limit=None and limit=5 on the same values
+re-masked with NaN runs of geometric length (p = 0.3).  One step = those 19 calls.
+
+Metric: algorithmic HBM bytes per second (GB/s) over the step, per function and in
+aggregate, as a fraction of the measured copy bandwidth.  Algorithmic bytes per
+call: grouped 8*R*M (values) + 4*M (labels, shared by the rows) + 8*R*K (output);
+fill 16*R*M (read + write).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+N > 1 runs one replica per GPU (launched with torchrun); the path has no exchange
+step, so ranks only synchronise around the timed region.  `--impl reference` times
+numbagg's algorithm on the host cores (the C restatement of its loops, OpenMP over
+rows like numba's parallel target) on a bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+ROWS = 64
+COLS = 16_777_216
+NAN_P = 0.05
+KS = (16, 4096, 1_000_000)
+GROUP_FUNCS = ("nansum", "nanmean", "nanvar", "nancount", "nanargmax")
+FILL_LIMITS = (None, 5)
+RUN_START_P = 0.015  # NaN-run starts per position for the fill input (runs ~Geometric(0.3))
+RUN_P = 0.3
+SAMPLE_COLS_CPU = 2_097_152  # bounded sample for the host-core timings (1/8 of the columns)
+METRIC = "HBM GB/s & % of peak per func; FP32-compensated vs FP64 speedup at stated err"
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cols", type=int, default=COLS, help="columns (smaller for quick runs)")
+    return p.parse_args(argv)
+
+
+# ---- multi-process helpers (replicas) ---------------------------------------------------
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value: float, device=None) -> float:
+    """Maximum of `value` over all ranks (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier():
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+# ---- workload ---------------------------------------------------------------------------
+
+
+def calls_and_bytes(rows: int, cols: int):
+    """(key, kind, args) for the 19 calls of one step, with algorithmic bytes."""
+    out = []
+    for K in KS:
+        for f in GROUP_FUNCS:
+            out.append((f"group_{f}_K{K}", ("group", f, K), 8 * rows * cols + 4 * cols + 8 * rows * K))
+    for lim in FILL_LIMITS:
+        for f in ("ffill", "bfill"):
+            out.append((f"{f}_limit{lim}", ("fill", f, lim), 16 * rows * cols))
+    return out
+
+
+def make_inputs(rows: int, cols: int, device):
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(1)
+    values = torch.randn((rows, cols), generator=g, dtype=torch.float64, device=device)
+    values[torch.rand((rows, cols), generator=g, device=device) < NAN_P] = float("nan")
+    labels = {}
+    for K in KS:
+        gk = torch.Generator(device=device)
+        gk.manual_seed(1000 + K)
+        labels[K] = torch.randint(0, K, (cols,), generator=gk, dtype=torch.int32, device=device)
+    # fill input: the same values re-masked with NaN runs of geometric length
+    fill = values.clone()
+    starts = torch.rand((rows, cols), generator=g, device=device) < RUN_START_P
+    r_idx, c_idx = torch.nonzero(starts, as_tuple=True)
+    del starts
+    u = torch.rand(r_idx.shape, generator=g, dtype=torch.float64, device=device).clamp_min(1e-300)
+    lengths = (torch.floor(torch.log(u) / math.log(1.0 - RUN_P)) + 1).to(torch.int64)  # Geometric(RUN_P)
+    ends = torch.clamp(c_idx + lengths, max=cols)
+    delta = torch.zeros((rows, cols + 1), dtype=torch.int32, device=device)
+    delta.index_put_((r_idx, c_idx), torch.ones_like(c_idx, dtype=torch.int32), accumulate=True)
+    delta.index_put_((r_idx, ends), -torch.ones_like(c_idx, dtype=torch.int32), accumulate=True)
+    covered = torch.cumsum(delta[:, :cols], dim=1) > 0
+    del delta
+    fill[covered] = float("nan")
+    del covered
+    return values, labels, fill
+
+
+def run_call(nb, spec, values, labels, fill):
+    kind, f, arg = spec
+    if kind == "group":
+        return getattr(nb, f"group_{f}")(values, labels[arg], num_labels=arg, axis=-1)
+    return getattr(nb, f)(fill, limit=arg)
+
+
+# ---- clocks ------------------------------------------------------------------------------
+
+
+class ClockSampler:
+    FIELDS = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL,
+                text=True,
+            )
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self._thread = threading.Thread(target=self._read, daemon=True)
+        self._thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._thread:
+            self._thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def measured_peak() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_for(key: str):
+    """DRAM bytes per launch of the dominant call, from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            data = json.load(fh)
+        return data.get(key)
+    except (OSError, ValueError):
+        return None
+
+
+# ---- CPU timing (oracle = numbagg's loops restated in C, OpenMP over rows) ---------------
+
+
+def cpu_step(values_np, labels_np, fill_np):
+    import oracle
+
+    t0 = time.perf_counter()
+    for K in KS:
+        lab = labels_np[K]
+        for f in GROUP_FUNCS:
+            oracle.group(f"group_{f}", values_np, lab, num_labels=K, axis=-1)
+    for lim in FILL_LIMITS:
+        for f in ("ffill", "bfill"):
+            oracle.fill(f, fill_np, limit=lim)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(values, labels, fill, cols):
+    sc = min(cols, SAMPLE_COLS_CPU)
+    v = values[:, :sc].cpu().numpy()
+    fl = fill[:, :sc].cpu().numpy()
+    lab = {K: labels[K][:sc].cpu().numpy() for K in KS}
+    return v, lab, fl, sc
+
+
+def sample_bytes(rows, sc):
+    return sum(b for _, _, b in calls_and_bytes(rows, sc))
+
+
+def sample_desc(rows, sc):
+    return (
+        f"{rows} x {sc} columns (first {sc} of {COLS}) of the same inputs, the 19 calls once; "
+        "numbagg's loops restated in C (oracle), OpenMP schedule(static) over rows"
+    )
+
+
+# ---- the reference arm --------------------------------------------------------------------
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    import oracle
+
+    oracle.lib()
+    rng = np.random.default_rng(1)
+    sc = min(args.cols, SAMPLE_COLS_CPU)
+    values = rng.standard_normal((ROWS, sc))
+    values[rng.random(values.shape) < NAN_P] = np.nan
+    fill = values.copy()
+    rr, cc = np.nonzero(rng.random(values.shape) < RUN_START_P)
+    ends = np.minimum(cc + rng.geometric(RUN_P, size=cc.shape), sc)
+    delta = np.zeros((ROWS, sc + 1), dtype=np.int32)
+    np.add.at(delta, (rr, cc), 1)
+    np.add.at(delta, (rr, ends), -1)
+    fill[np.cumsum(delta[:, :sc], axis=1) > 0] = np.nan
+    labels = {K: rng.integers(0, K, size=sc).astype(np.int32) for K in KS}
+    for _ in range(args.warmup):
+        cpu_step(values, labels, fill)
+    t = 0.0
+    for _ in range(args.steps):
+        t += cpu_step(values, labels, fill)
+    ms = 1000.0 * t / max(args.steps, 1)
+    gbs = sample_bytes(ROWS, sc) / (ms / 1000.0) / 1e9
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": gbs,
+        "unit": "GB/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": workload_config(ROWS, args.cols),
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample_desc(ROWS, sc)},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(rows, cols):
+    return {
+        "workload": f"group_nan{{sum,mean,var,count,argmax}} x K in {list(KS)} + ffill/bfill limit in [None, 5]; "
+        f"float64 values {rows}x{cols}, 5% NaN; int32 labels",
+        "rows": rows,
+        "cols": cols,
+        "num_labels": list(KS),
+        "fill_nan_runs": f"starts Bernoulli({RUN_START_P}) per position, length Geometric({RUN_P})",
+        "l2": "inputs larger than L2 (each float64 array is 8.6 GB, L2 is 129 MB)",
+        "parallelism": "replicas",
+    }
+
+
+# ---- our arm --------------------------------------------------------------------------------
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+    import numbagg_gb300 as nb
+    from numbagg_gb300 import _lib
+
+    rows, cols = ROWS, args.cols
+    values, labels, fill = make_inputs(rows, cols, device)
+    calls = calls_and_bytes(rows, cols)
+    torch.cuda.synchronize(device)
+
+    for _ in range(args.warmup):
+        for _, spec, _ in calls:
+            run_call(nb, spec, values, labels, fill)
+    torch.cuda.synchronize(device)
+
+    stream = torch.cuda.current_stream(device)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(args.steps)]
+    sampler = ClockSampler(device.index or 0)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize(device)
+    launches0 = _lib.launch_count()
+    for s in range(args.steps):
+        ev[s][0].record(stream)
+        for i, (_, spec, _) in enumerate(calls):
+            run_call(nb, spec, values, labels, fill)
+            ev[s][i + 1].record(stream)
+    torch.cuda.synchronize(device)
+    barrier()
+    launches = _lib.launch_count() - launches0
+    clocks = sampler.stop()
+
+    per_call_ms = [0.0] * len(calls)
+    total_ms = 0.0
+    for s in range(args.steps):
+        total_ms += ev[s][0].elapsed_time(ev[s][-1])
+        for i in range(len(calls)):
+            per_call_ms[i] += ev[s][i].elapsed_time(ev[s][i + 1])
+    ms_step = total_ms / args.steps
+    ms_step = reduce_max(ms_step, device)
+    step_bytes = sum(b for _, _, b in calls)
+    value = world * step_bytes / (ms_step / 1000.0) / 1e9
+
+    peak, peak_kind = measured_peak()
+    per_func = {}
+    for (key, _, b), t in zip(calls, per_call_ms):
+        avg = t / args.steps
+        gbs = b / (avg / 1000.0) / 1e9
+        per_func[key] = {"ms": round(avg, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    dom = max(range(len(calls)), key=lambda i: per_call_ms[i])
+    dom_key, _, dom_bytes = calls[dom]
+    dom_ms = per_call_ms[dom] / args.steps
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "kernel": dom_key,
+        "achieved": round(achieved, 1),
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": round(achieved / peak, 4),
+        "traffic": traffic_for(dom_key),
+        "bytes_per_launch": dom_bytes,
+    }
+
+    e2e = None
+    if not args.no_e2e and args.e2e_steps > 0:
+        e2e = run_e2e(args, nb, values, labels, fill, calls, device, world)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and world == 1:
+        v, lab, fl, sc = cpu_sample(values, labels, fill, cols)
+        import oracle
+
+        oracle.lib()
+        t = cpu_step(v, lab, fl)
+        cpu = {
+            "value": round(sample_bytes(rows, sc) / t / 1e9, 2),
+            "unit": "GB/s",
+            "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": sample_desc(rows, sc),
+        }
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": round(value, 1),
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_step, 3),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": workload_config(rows, cols),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "per_func": per_func,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, nb, values, labels, fill, calls, device, world):
+    """The same step through the public API with host buffers: every step copies its
+    inputs from pinned host memory and reads every result back into pinned memory."""
+    import torch
+
+    h_values = torch.empty(values.shape, dtype=values.dtype, pin_memory=True)
+    h_fill = torch.empty(fill.shape, dtype=fill.dtype, pin_memory=True)
+    h_values.copy_(values)
+    h_fill.copy_(fill)
+    h_labels = {K: torch.empty(labels[K].shape, dtype=labels[K].dtype, pin_memory=True).copy_(labels[K]) for K in KS}
+    out_bytes = {}
+    h_out_fill = torch.empty(fill.shape, dtype=fill.dtype, pin_memory=True)
+    h_out_group = {K: torch.empty((values.shape[0], K), dtype=torch.float64, pin_memory=True) for K in KS}
+    stream = torch.cuda.current_stream(device)
+    h2d = values.numel() * 8 + fill.numel() * 8 + sum(labels[K].numel() * 4 for K in KS)
+    d2h = 0
+    for _, (kind, f, arg), _ in calls:
+        d2h += fill.numel() * 8 if kind == "fill" else values.shape[0] * arg * 8
+    del out_bytes
+
+    def step():
+        d_values = h_values.to(device, non_blocking=True)
+        d_fill = h_fill.to(device, non_blocking=True)
+        d_labels = {K: h_labels[K].to(device, non_blocking=True) for K in KS}
+        for _, spec, _ in calls:
+            r = run_call(nb, spec, d_values, d_labels, d_fill)
+            kind, f, arg = spec
+            (h_out_fill if kind == "fill" else h_out_group[arg]).copy_(r, non_blocking=True)
+        return d_values, d_fill
+
+    step()
+    torch.cuda.synchronize(device)
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.e2e_steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize(device)
+    barrier()
+    ms = reduce_max(t0.elapsed_time(t1) / args.e2e_steps, device)
+    step_bytes = sum(b for _, _, b in calls)
+    return {
+        "value": round(world * step_bytes / (ms / 1000.0) / 1e9, 1),
+        "unit": "GB/s",
+        "h2d_bytes_per_step": int(h2d),
+        "d2h_bytes_per_step": int(d2h),
+        "ms_per_step": round(ms, 3),
+        "steps": args.e2e_steps,
+    }
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

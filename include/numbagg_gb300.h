@@ -1,0 +1,180 @@
+/*
+ * numbagg_gb300 -- C ABI of the GB300 (sm_103a) scan / reduction library.
+ *
+ * Every entry point replaces one numba gufunc of numbagg: the decorator's
+ * `__call__` (argument checks, axis handling) stays on the host, and what the
+ * gufunc computed over the loop dimensions is one call here over a (rows, n)
+ * C-contiguous view with the scanned axis last.  Plain pointers and sizes only:
+ * device pointers for data, `stream` is a cudaStream_t (NULL = legacy default).
+ * Calls are asynchronous on `stream`; every call returns an NBG_* status.
+ *
+ * Workspaces.  Scans along a row (moving windows, exponential moving functions,
+ * fills) carry state between tiles through a workspace sized by the matching
+ * *_workspace_bytes() query.  A scan workspace must be zero-filled once when it is
+ * allocated; it then maintains itself across launches.  One workspace per stream:
+ * launches that share a workspace must be ordered on one stream.  Grouped
+ * reductions take a scratch buffer sized by nbg_group_workspace_bytes() that needs
+ * no initialisation (do not share it with a scan workspace).
+ */
+#ifndef NUMBAGG_GB300_H
+#define NUMBAGG_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__) || defined(__clang__)
+#define NBG_API __attribute__((visibility("default")))
+#else
+#define NBG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define NBG_OK 0
+#define NBG_INVALID_ARGUMENT 1 /* numbagg raises ValueError/TypeError before compute */
+#define NBG_LAUNCH_ERROR 2
+#define NBG_WORKSPACE_TOO_SMALL 3
+#define NBG_LOOKBACK_TIMEOUT 4 /* recorded on the device; read with nbg_workspace_error */
+#define NBG_UNSUPPORTED 5
+
+NBG_API int nbg_version(void);
+NBG_API const char* nbg_status_string(int status);
+NBG_API size_t nbg_workspace_header_bytes(void);
+NBG_API int nbg_workspace_error(void* ws, int* code, unsigned* tile, void* stream);
+/* Number of kernels this library has launched in the process (all devices). */
+NBG_API unsigned long long nbg_launch_count(void);
+/* Test hook for failure detection: one bounded wait on a status nothing publishes. */
+NBG_API int nbg_debug_lookback_timeout(void* ws, size_t ws_bytes, int spin_limit, void* stream);
+
+/* ---- moving windows ---------------------------------------------------------------
+ * Replaces the gufuncs built by ndmove (numbagg/decorators.py:275-341) from
+ *   move_sum  numbagg/moving.py:58-99      move_mean numbagg/moving.py:12-55
+ *   move_var  numbagg/moving.py:154-181    move_std  numbagg/moving.py:123-151
+ *   move_cov  numbagg/moving.py:184-220    move_corr numbagg/moving.py:223-275
+ * signature "(a),(),()->(a)" / "(a),(a),(),()->(a)"; a, b, out: rows x n.
+ * min_count is passed unclamped (each kernel applies the reference's max()). */
+NBG_API size_t nbg_move_workspace_bytes(long long rows, long long n);
+#define NBG_DECL_MOVE1(NAME, T, SFX)                                                      \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window, \
+                         long long min_count, void* ws, size_t ws_bytes, void* stream);
+#define NBG_DECL_MOVE2(NAME, T, SFX)                                                      \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, const T* b, T* out, long long rows, long long n,      \
+                         long long window, long long min_count, void* ws, size_t ws_bytes, \
+                         void* stream);
+NBG_DECL_MOVE1(move_sum, double, f64)
+NBG_DECL_MOVE1(move_sum, float, f32)
+NBG_DECL_MOVE1(move_mean, double, f64)
+NBG_DECL_MOVE1(move_mean, float, f32)
+NBG_DECL_MOVE1(move_var, double, f64)
+NBG_DECL_MOVE1(move_var, float, f32)
+NBG_DECL_MOVE1(move_std, double, f64)
+NBG_DECL_MOVE1(move_std, float, f32)
+NBG_DECL_MOVE2(move_cov, double, f64)
+NBG_DECL_MOVE2(move_cov, float, f32)
+NBG_DECL_MOVE2(move_corr, double, f64)
+NBG_DECL_MOVE2(move_corr, float, f32)
+
+/* ---- exponentially weighted moving functions ---------------------------------------
+ * Replaces the gufuncs built by ndmoveexp (numbagg/decorators.py:344-414) from
+ *   move_exp_nancount numbagg/moving_exp.py:12-38    move_exp_nanmean numbagg/moving_exp.py:41-71
+ *   move_exp_nansum   numbagg/moving_exp.py:74-102   move_exp_nanvar  numbagg/moving_exp.py:105-156
+ *   move_exp_nanstd   numbagg/moving_exp.py:158-223  move_exp_nancov  numbagg/moving_exp.py:226-272
+ *   move_exp_nancorr  numbagg/moving_exp.py:275-335
+ * alpha_mode 0: scalar alpha_scalar (already rounded to the array dtype);
+ * 1: `alpha` holds n values shared by every row; 2: `alpha` holds rows x n values.
+ * min_weight is the array-dtype value widened to double. */
+NBG_API size_t nbg_move_exp_workspace_bytes(long long rows, long long n);
+#define NBG_DECL_EXP1(NAME, T, SFX)                                                         \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, const T* alpha, double alpha_scalar, int alpha_mode,    \
+                         double min_weight, T* out, long long rows, long long n, void* ws,   \
+                         size_t ws_bytes, void* stream);
+#define NBG_DECL_EXP2(NAME, T, SFX)                                                         \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,        \
+                         int alpha_mode, double min_weight, T* out, long long rows,          \
+                         long long n, void* ws, size_t ws_bytes, void* stream);
+NBG_DECL_EXP1(move_exp_nancount, double, f64)
+NBG_DECL_EXP1(move_exp_nancount, float, f32)
+NBG_DECL_EXP1(move_exp_nanmean, double, f64)
+NBG_DECL_EXP1(move_exp_nanmean, float, f32)
+NBG_DECL_EXP1(move_exp_nansum, double, f64)
+NBG_DECL_EXP1(move_exp_nansum, float, f32)
+NBG_DECL_EXP1(move_exp_nanvar, double, f64)
+NBG_DECL_EXP1(move_exp_nanvar, float, f32)
+NBG_DECL_EXP1(move_exp_nanstd, double, f64)
+NBG_DECL_EXP1(move_exp_nanstd, float, f32)
+NBG_DECL_EXP2(move_exp_nancov, double, f64)
+NBG_DECL_EXP2(move_exp_nancov, float, f32)
+NBG_DECL_EXP2(move_exp_nancorr, double, f64)
+NBG_DECL_EXP2(move_exp_nancorr, float, f32)
+
+/* ---- fills --------------------------------------------------------------------------
+ * Replaces the gufuncs built by ndfill (numbagg/decorators.py:417-487) from
+ *   ffill numbagg/funcs.py:313-326    bfill numbagg/funcs.py:294-311
+ * signature "(n),()->(n)"; limit >= 0 (numbagg passes shape[axis] for None).
+ * Integer arrays need no workspace. */
+NBG_API size_t nbg_fill_workspace_bytes(long long rows, long long n);
+#define NBG_DECL_FILL(T, SFX)                                                                \
+  NBG_API int nbg_ffill_##SFX(const T* a, T* out, long long rows, long long n, long long limit,       \
+                      void* ws, size_t ws_bytes, void* stream);                              \
+  NBG_API int nbg_bfill_##SFX(const T* a, T* out, long long rows, long long n, long long limit,       \
+                      void* ws, size_t ws_bytes, void* stream);
+NBG_DECL_FILL(double, f64)
+NBG_DECL_FILL(float, f32)
+NBG_DECL_FILL(int, i32)
+NBG_DECL_FILL(long long, i64)
+
+/* ---- grouped reductions ----------------------------------------------------------------
+ * Replaces the gufuncs built by groupndreduce (numbagg/decorators.py:490-674) from
+ * numbagg/grouped.py:7-270: values rows x m (the broadcast dims flattened, the core
+ * dims flattened in C order), labels m (shared by every row), out rows x num_labels.
+ * Labels < 0 or >= num_labels are skipped.  ddof is read by nanvar/nanstd only.
+ * `func` for the workspace query: 0 sum, 1 count, 2 mean, 3 var, 4 std, 5 sum_of_squares,
+ * 6 argmax, 7 argmin, 8 max, 9 min, 10 first, 11 last, 12 prod, 13 any, 14 all. */
+NBG_API size_t nbg_group_workspace_bytes(int func, long long rows, long long m, long long num_labels);
+#define NBG_DECL_GROUP1(NAME, V, VS, O, L, LS)                                                 \
+  NBG_API int nbg_group_##NAME##_##VS##_##LS(const V* values, const L* labels, O* out, long long rows,  \
+                                     long long m, long long num_labels, long long ddof,        \
+                                     void* ws, size_t ws_bytes, void* stream);
+#define NBG_DECL_GROUP_L(NAME, V, VS, O) \
+  NBG_DECL_GROUP1(NAME, V, VS, O, int, i32) NBG_DECL_GROUP1(NAME, V, VS, O, long long, i64)
+#define NBG_DECL_GROUP_ALL(NAME)                                                   \
+  NBG_DECL_GROUP_L(NAME, double, f64, double) NBG_DECL_GROUP_L(NAME, float, f32, float) \
+  NBG_DECL_GROUP_L(NAME, int, i32, int) NBG_DECL_GROUP_L(NAME, long long, i64, long long)
+#define NBG_DECL_GROUP_FLOAT(NAME) \
+  NBG_DECL_GROUP_L(NAME, double, f64, double) NBG_DECL_GROUP_L(NAME, float, f32, float)
+NBG_DECL_GROUP_ALL(nansum)            /* numbagg/grouped.py:30-40 */
+NBG_DECL_GROUP_ALL(nancount)          /* numbagg/grouped.py:43-51 */
+NBG_DECL_GROUP_FLOAT(nanmean)         /* numbagg/grouped.py:7-27 (ints promoted by the caller) */
+NBG_DECL_GROUP_FLOAT(nanvar)          /* numbagg/grouped.py:148-176 */
+NBG_DECL_GROUP_FLOAT(nanstd)          /* numbagg/grouped.py:179-208 */
+NBG_DECL_GROUP_ALL(nansum_of_squares) /* numbagg/grouped.py:135-145 */
+NBG_DECL_GROUP_ALL(nanargmax)         /* numbagg/grouped.py:54-75 */
+NBG_DECL_GROUP_ALL(nanargmin)         /* numbagg/grouped.py:78-92 */
+NBG_DECL_GROUP_ALL(nanmax)            /* numbagg/grouped.py:229-244 */
+NBG_DECL_GROUP_ALL(nanmin)            /* numbagg/grouped.py:211-226 */
+NBG_DECL_GROUP_ALL(nanfirst)          /* numbagg/grouped.py:95-110 */
+NBG_DECL_GROUP_ALL(nanlast)           /* numbagg/grouped.py:113-121 */
+NBG_DECL_GROUP_ALL(nanprod)           /* numbagg/grouped.py:124-132 */
+NBG_DECL_GROUP_ALL(nanany)            /* numbagg/grouped.py:247-257 */
+NBG_DECL_GROUP_ALL(nanall)            /* numbagg/grouped.py:260-270 */
+
+/* ---- moving covariance / correlation matrices ----------------------------------------
+ * Replaces the gufuncs built by ndmovematrix (numbagg/decorators.py:747-818) from
+ *   move_corrmatrix numbagg/moving_matrix.py:16-114
+ *   move_covmatrix  numbagg/moving_matrix.py:117-201
+ * signature "(m,n),(),()->(m,n,n)": a batch x n_obs x n_vars, out batch x n_obs x n_vars x n_vars. */
+#define NBG_DECL_MATRIX(NAME, T, SFX)                                                           \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long batch, long long n_obs, long long n_vars, \
+                         long long window, long long min_count, void* stream);
+NBG_DECL_MATRIX(move_covmatrix, double, f64)
+NBG_DECL_MATRIX(move_covmatrix, float, f32)
+NBG_DECL_MATRIX(move_corrmatrix, double, f64)
+NBG_DECL_MATRIX(move_corrmatrix, float, f32)
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUMBAGG_GB300_H */

@@ -1,0 +1,515 @@
+// Labelled reductions group_nan* (numbagg/grouped.py:7-270).
+//
+// values (rows, m), labels (m,) shared by every row, out (rows, K).  A label < 0 is
+// skipped (numbagg/grouped.py:14); a label >= K is skipped as well (numba would write
+// out of bounds there, so the reference leaves it undefined).
+//
+// Two strategies, picked on the host from K:
+//   * shared-memory bins (K * 24 B fits in shared memory): a CTA owns one column
+//     chunk of one row and accumulates into bins in shared memory, replicated per
+//     lane (no atomics) for tiny K, per warp for small K, or per CTA; at the end it
+//     writes one partial state per bin.  A second kernel folds the partials over the
+//     chunks in chunk order and writes the output, so results repeat run to run.
+//   * global bins (large K, e.g. 10^6 labels): atomics into an accumulator in the
+//     workspace, then the same fold/finalise kernel with one chunk.
+//
+// Selection kernels keep numbagg's float64 running extreme with a strict comparison
+// (first index wins on ties, numbagg/grouped.py:62, :86, :221, :239).  Here every
+// element becomes an order key of its float64 value in which -0.0 == +0.0; a first
+// sweep takes the maximum key per bin and a second sweep the minimum column index
+// among the elements holding that key.  The (key, first index) pair is exactly the
+// sequential result, so argmax/argmin/max/min/first/last are bit-exact.
+//
+// Integer sums, products and sums of squares wrap modulo 2^64 and are truncated to
+// the output type, which equals numba's int64 arithmetic stored into the narrow
+// output; integer results are therefore exact in any order.
+#include "nbg_common.cuh"
+
+#include <climits>
+
+namespace nbg {
+namespace grouped {
+
+enum Func : int {
+  kSum = 0,
+  kCount,
+  kMean,
+  kVar,
+  kStd,
+  kSumSq,
+  kArgMax,
+  kArgMin,
+  kMax,
+  kMin,
+  kFirst,
+  kLast,
+  kProd,
+  kAny,
+  kAll,
+  kNumFuncs
+};
+
+struct Acc {  // one bin: meaning depends on the function family
+  unsigned long long a, b, c;
+};
+
+constexpr unsigned long long kNoIdx = ~0ull;
+
+NBG_HOST_DEVICE bool is_moments(int f) {
+  return f == kSum || f == kCount || f == kMean || f == kVar || f == kStd || f == kSumSq;
+}
+NBG_HOST_DEVICE bool is_select(int f) { return f == kArgMax || f == kArgMin || f == kMax || f == kMin; }
+
+template <typename V>
+struct IsFloat { static constexpr bool value = false; };
+template <>
+struct IsFloat<double> { static constexpr bool value = true; };
+template <>
+struct IsFloat<float> { static constexpr bool value = true; };
+
+template <int F>
+NBG_DEVICE Acc acc_identity() {
+  Acc r{0ull, 0ull, 0ull};
+  if (is_select(F) || F == kFirst) r.b = kNoIdx;
+  if (F == kFirst) r.a = kNoIdx;
+  if (F == kProd) r.a = 0;  // set per value type in init (1 or 1.0)
+  if (F == kAll) r.a = 1ull;
+  return r;
+}
+
+template <int F, typename V>
+NBG_DEVICE Acc acc_init() {
+  Acc r = acc_identity<F>();
+  if (F == kProd) {
+    if (IsFloat<V>::value)
+      r.a = static_cast<unsigned long long>(__double_as_longlong(1.0));
+    else
+      r.a = 1ull;
+  }
+  return r;
+}
+
+template <typename V>
+NBG_DEVICE unsigned long long select_key(V v, bool minimize) {
+  const unsigned long long k = order_key_ieee(static_cast<double>(v));
+  return minimize ? ~k : k;
+}
+
+NBG_DEVICE double as_d(unsigned long long u) { return __longlong_as_double(static_cast<long long>(u)); }
+NBG_DEVICE unsigned long long as_u(double d) { return static_cast<unsigned long long>(__double_as_longlong(d)); }
+
+// Shared-memory double add: compare-and-swap on the bit pattern.
+NBG_DEVICE void atomic_add_f64(unsigned long long* p, double v) {
+  atomicAdd(reinterpret_cast<double*>(p), v);
+}
+
+template <typename V>
+NBG_DEVICE void atomic_mul(unsigned long long* p, V v) {
+  unsigned long long old = *p, assumed;
+  do {
+    assumed = old;
+    unsigned long long nv;
+    if (IsFloat<V>::value)
+      nv = as_u(as_d(assumed) * static_cast<double>(v));
+    else
+      nv = assumed * static_cast<unsigned long long>(static_cast<long long>(v));
+    old = atomicCAS(p, assumed, nv);
+  } while (old != assumed);
+}
+
+// Accumulate one valid element into a bin.  ATOMIC selects atomics vs plain RMW
+// (lane-private bins).
+template <int F, typename V, bool ATOMIC>
+NBG_DEVICE void accumulate(Acc* bin, V v, unsigned long long col) {
+  if (is_moments(F)) {
+    const bool need_s1 = F == kSum || F == kMean || F == kVar || F == kStd;
+    const bool need_s2 = F == kVar || F == kStd || F == kSumSq;
+    const bool need_c = F == kCount || F == kMean || F == kVar || F == kStd;
+    if (IsFloat<V>::value) {
+      const double x = static_cast<double>(v);
+      if (ATOMIC) {
+        if (need_s1) atomic_add_f64(&bin->a, x);
+        if (need_s2) atomic_add_f64(&bin->b, x * x);
+        if (need_c) atomicAdd(&bin->c, 1ull);
+      } else {
+        if (need_s1) bin->a = as_u(as_d(bin->a) + x);
+        if (need_s2) bin->b = as_u(as_d(bin->b) + x * x);
+        if (need_c) bin->c += 1ull;
+      }
+    } else {
+      const unsigned long long x = static_cast<unsigned long long>(static_cast<long long>(v));
+      if (ATOMIC) {
+        if (need_s1) atomicAdd(&bin->a, x);
+        if (need_s2) atomicAdd(&bin->b, x * x);
+        if (need_c) atomicAdd(&bin->c, 1ull);
+      } else {
+        if (need_s1) bin->a += x;
+        if (need_s2) bin->b += x * x;
+        if (need_c) bin->c += 1ull;
+      }
+    }
+  } else if (F == kFirst) {
+    if (ATOMIC) atomicMin(&bin->a, col); else if (col < bin->a) bin->a = col;
+  } else if (F == kLast) {
+    if (ATOMIC) atomicMax(&bin->a, col + 1); else if (col + 1 > bin->a) bin->a = col + 1;
+  } else if (F == kProd) {
+    if (ATOMIC) {
+      atomic_mul<V>(&bin->a, v);
+    } else {
+      if (IsFloat<V>::value)
+        bin->a = as_u(as_d(bin->a) * static_cast<double>(v));
+      else
+        bin->a = bin->a * static_cast<unsigned long long>(static_cast<long long>(v));
+    }
+  } else if (F == kAny) {
+    if (v != V(0)) {
+      if (ATOMIC) atomicOr(reinterpret_cast<unsigned*>(&bin->a), 1u); else bin->a = 1ull;
+    }
+  } else if (F == kAll) {
+    if (v == V(0)) {
+      if (ATOMIC) atomicAnd(reinterpret_cast<unsigned*>(&bin->a), 0u); else bin->a = 0ull;
+    }
+  } else if (is_select(F)) {
+    const unsigned long long key = select_key(v, F == kArgMin || F == kMin);
+    if (ATOMIC) atomicMax(&bin->a, key); else if (key > bin->a) bin->a = key;
+  }
+}
+
+// Fold bin `src` into `dst` (dst earlier in column order than src).
+template <int F, typename V>
+NBG_DEVICE Acc fold(Acc dst, const Acc& src) {
+  if (is_moments(F)) {
+    if (IsFloat<V>::value) {
+      dst.a = as_u(as_d(dst.a) + as_d(src.a));
+      dst.b = as_u(as_d(dst.b) + as_d(src.b));
+    } else {
+      dst.a += src.a;
+      dst.b += src.b;
+    }
+    dst.c += src.c;
+  } else if (is_select(F)) {
+    if (src.a > dst.a || (src.a == dst.a && src.b < dst.b)) dst = src;
+  } else if (F == kFirst) {
+    if (src.a < dst.a) dst.a = src.a;
+  } else if (F == kLast) {
+    if (src.a > dst.a) dst.a = src.a;
+  } else if (F == kProd) {
+    if (IsFloat<V>::value)
+      dst.a = as_u(as_d(dst.a) * as_d(src.a));
+    else
+      dst.a = dst.a * src.a;
+  } else if (F == kAny) {
+    dst.a |= src.a;
+  } else if (F == kAll) {
+    dst.a &= src.a;
+  }
+  return dst;
+}
+
+template <typename V>
+NBG_DEVICE V load_value(const V* p) { return *p; }
+
+constexpr int NT = 256;
+
+// ---- shared-memory strategy -------------------------------------------------------
+// grid (chunks, rows).  REP replicas of the K bins: 1 (per CTA), NT/32 (per warp) or
+// NT (per thread, plain read-modify-write).
+template <int F, typename V, typename L, int REP>
+__global__ void __launch_bounds__(NT) accum_smem(const V* __restrict__ values,
+                                                 const L* __restrict__ labels, long long m,
+                                                 long long K, long long chunk_len,
+                                                 Acc* __restrict__ partials) {
+  extern __shared__ Acc bins[];
+  const long long row = blockIdx.y;
+  const long long chunk = blockIdx.x;
+  const long long col0 = chunk * chunk_len;
+  long long col1 = col0 + chunk_len;
+  if (col1 > m) col1 = m;
+  const long long nbins = K * REP;
+  for (long long j = threadIdx.x; j < nbins; j += NT) bins[j] = acc_init<F, V>();
+  __syncthreads();
+  const int rep = REP == 1 ? 0 : (REP == NT ? threadIdx.x : (threadIdx.x >> 5));
+  Acc* my = bins + static_cast<long long>(rep) * K;
+  const V* vr = values + row * m;
+  constexpr bool ATOMIC = REP != NT;
+  for (long long col = col0 + threadIdx.x; col < col1; col += NT) {
+    const long long lab = static_cast<long long>(labels[col]);
+    if (lab < 0 || lab >= K) continue;
+    const V v = vr[col];
+    if (is_nan(v)) continue;
+    accumulate<F, V, ATOMIC>(my + lab, v, static_cast<unsigned long long>(col));
+  }
+  __syncthreads();
+  if (is_select(F)) {
+    // second sweep: first column holding the bin's extreme key
+    for (long long col = col0 + threadIdx.x; col < col1; col += NT) {
+      const long long lab = static_cast<long long>(labels[col]);
+      if (lab < 0 || lab >= K) continue;
+      const V v = vr[col];
+      if (is_nan(v)) continue;
+      const unsigned long long key = select_key(v, F == kArgMin || F == kMin);
+      if (key == my[lab].a) atomicMin(&my[lab].b, static_cast<unsigned long long>(col));
+    }
+    __syncthreads();
+  }
+  Acc* out = partials + (row * gridDim.x + chunk) * K;
+  for (long long k = threadIdx.x; k < K; k += NT) {
+    Acc r = bins[k];
+    for (int j = 1; j < REP; ++j) r = fold<F, V>(r, bins[static_cast<long long>(j) * K + k]);
+    out[k] = r;
+  }
+}
+
+// ---- global strategy -----------------------------------------------------------------
+template <int F, typename V>
+__global__ void init_global(Acc* __restrict__ acc, long long total) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride)
+    acc[i] = acc_init<F, V>();
+}
+
+// grid (chunks, rows); PASS 0 accumulates, PASS 1 is the select tie sweep
+template <int F, typename V, typename L, int PASS>
+__global__ void __launch_bounds__(NT) accum_global(const V* __restrict__ values,
+                                                   const L* __restrict__ labels, long long m,
+                                                   long long K, long long chunk_len,
+                                                   Acc* __restrict__ acc) {
+  const long long row = blockIdx.y;
+  const long long col0 = static_cast<long long>(blockIdx.x) * chunk_len;
+  long long col1 = col0 + chunk_len;
+  if (col1 > m) col1 = m;
+  const V* vr = values + row * m;
+  Acc* ar = acc + row * K;
+  for (long long col = col0 + threadIdx.x; col < col1; col += NT) {
+    const long long lab = static_cast<long long>(labels[col]);
+    if (lab < 0 || lab >= K) continue;
+    const V v = vr[col];
+    if (is_nan(v)) continue;
+    if (PASS == 0) {
+      accumulate<F, V, true>(ar + lab, v, static_cast<unsigned long long>(col));
+    } else {
+      const unsigned long long key = select_key(v, F == kArgMin || F == kMin);
+      if (key == ar[lab].a) atomicMin(&ar[lab].b, static_cast<unsigned long long>(col));
+    }
+  }
+}
+
+// ---- fold partials over chunks and write the output --------------------------------
+template <typename O>
+NBG_DEVICE O nan_of() {
+  if (IsFloat<O>::value) return static_cast<O>(__longlong_as_double(0x7ff8000000000000ll));
+  return sizeof(O) == 4 ? static_cast<O>(INT_MIN) : static_cast<O>(LLONG_MIN);
+}
+
+template <int F, typename V, typename O>
+__global__ void finalize(const Acc* __restrict__ partials, const V* __restrict__ values,
+                         O* __restrict__ out, long long rows, long long m, long long K,
+                         long long chunks, long long ddof) {
+  const long long total = rows * K;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long row = t / K, k = t - row * K;
+    Acc r = acc_init<F, V>();
+    for (long long c = 0; c < chunks; ++c) r = fold<F, V>(r, partials[(row * chunks + c) * K + k]);
+    O res;
+    if (F == kSum) {
+      res = IsFloat<V>::value ? static_cast<O>(as_d(r.a)) : static_cast<O>(static_cast<long long>(r.a));
+    } else if (F == kSumSq) {
+      res = IsFloat<V>::value ? static_cast<O>(as_d(r.b)) : static_cast<O>(static_cast<long long>(r.b));
+    } else if (F == kCount) {
+      res = static_cast<O>(r.c);
+    } else if (F == kMean) {
+      // out[label] /= count   (numbagg/grouped.py:22-27)
+      res = r.c == 0 ? nan_of<O>() : static_cast<O>(as_d(r.a) / static_cast<double>(r.c));
+    } else if (F == kVar || F == kStd) {
+      // (sums_of_squares - sums**2 / count) / (count - ddof)   numbagg/grouped.py:170-176
+      const long long cnt = static_cast<long long>(r.c);
+      const long long denom = cnt - ddof;
+      if (denom <= 0) {
+        res = nan_of<O>();
+      } else {
+        const double s = as_d(r.a);
+        double v = (as_d(r.b) - (s * s) / static_cast<double>(cnt)) / static_cast<double>(denom);
+        if (F == kStd) v = sqrt(v);
+        res = static_cast<O>(v);
+      }
+    } else if (F == kArgMax || F == kArgMin) {
+      res = r.b == kNoIdx ? nan_of<O>() : static_cast<O>(r.b);
+    } else if (F == kMax || F == kMin) {
+      res = r.b == kNoIdx ? nan_of<O>()
+                          : static_cast<O>(static_cast<double>(values[row * m + static_cast<long long>(r.b)]));
+    } else if (F == kFirst) {
+      if (r.a == kNoIdx)
+        res = IsFloat<O>::value ? nan_of<O>() : O(0);
+      else
+        res = static_cast<O>(values[row * m + static_cast<long long>(r.a)]);
+    } else if (F == kLast) {
+      res = r.a == 0 ? nan_of<O>() : static_cast<O>(values[row * m + static_cast<long long>(r.a) - 1]);
+    } else if (F == kProd) {
+      res = IsFloat<V>::value ? static_cast<O>(as_d(r.a)) : static_cast<O>(static_cast<long long>(r.a));
+    } else {  // kAny, kAll
+      res = static_cast<O>(r.a & 1ull);
+    }
+    out[t] = res;
+  }
+}
+
+}  // namespace grouped
+}  // namespace nbg
+
+using namespace nbg;
+using namespace nbg::grouped;
+
+namespace {
+
+int num_sms() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+constexpr size_t kSmemBudget = 96 * 1024;
+
+int replicas_for(long long K, int f) {
+  // lane-private bins need no atomics; selection needs one replica for the tie sweep
+  if (is_select(f)) return 1;
+  if (K * static_cast<long long>(sizeof(Acc)) * NT <= static_cast<long long>(kSmemBudget)) return NT;
+  if (K * static_cast<long long>(sizeof(Acc)) * (NT / 32) <= static_cast<long long>(kSmemBudget)) return NT / 32;
+  return 1;
+}
+
+bool use_smem(long long K) { return K * static_cast<long long>(sizeof(Acc)) <= static_cast<long long>(kSmemBudget); }
+
+struct Plan {
+  bool smem;
+  int rep;
+  long long chunks, chunk_len;
+};
+
+Plan make_plan(int f, long long rows, long long m, long long K) {
+  Plan p;
+  p.smem = use_smem(K);
+  p.rep = p.smem ? replicas_for(K, f) : 1;
+  const long long target_ctas = static_cast<long long>(num_sms()) * 4;
+  long long chunks = (target_ctas + rows - 1) / (rows > 0 ? rows : 1);
+  // a chunk should be long enough to amortise initialising and flushing its bins
+  const long long min_len = p.smem ? (K * 4 > 4096 ? K * 4 : 4096) : 8192;
+  const long long max_chunks = (m + min_len - 1) / min_len;
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks < 1) chunks = 1;
+  if (chunks > 65535) chunks = 65535;
+  p.chunk_len = (m + chunks - 1) / chunks;
+  p.chunks = (m + p.chunk_len - 1) / p.chunk_len;
+  if (p.chunks < 1) p.chunks = 1;
+  return p;
+}
+
+size_t plan_bytes(const Plan& p, long long rows, long long K) {
+  const long long slots = p.smem ? rows * p.chunks * K : rows * K;
+  return static_cast<size_t>(slots) * sizeof(Acc) + 256;
+}
+
+template <int F, typename V, typename L, int REP>
+cudaError_t run_smem(const V* values, const L* labels, long long rows, long long m, long long K,
+                     const Plan& p, Acc* acc, cudaStream_t s) {
+  const size_t smem = static_cast<size_t>(K) * REP * sizeof(Acc);
+  auto kern = accum_smem<F, V, L, REP>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  dim3 grid(static_cast<unsigned>(p.chunks), static_cast<unsigned>(rows));
+  kern<<<grid, NT, smem, s>>>(values, labels, m, K, p.chunk_len, acc);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+template <int F, typename V, typename L, typename O>
+int launch_group(const V* values, const L* labels, O* out, long long rows, long long m, long long K,
+                 long long ddof, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (rows < 0 || m < 0 || K < 0) return kInvalidArgument;
+  if (rows == 0 || K == 0) return kOk;
+  if (rows > 65535) return kUnsupported;
+  if (!out || (m > 0 && (!values || !labels))) return kInvalidArgument;
+  const Plan p = make_plan(F, rows, m, K);
+  if (!ws || ws_bytes < plan_bytes(p, rows, K)) return kWorkspaceTooSmall;
+  Acc* acc = static_cast<Acc*>(ws);
+  cudaError_t e = cudaSuccess;
+  long long fold_chunks = 1;
+  if (m == 0) {
+    init_global<F, V><<<64, 256, 0, s>>>(acc, rows * K);
+    note_launches(1);
+  } else if (p.smem) {
+    fold_chunks = p.chunks;
+    if (p.rep == NT) e = run_smem<F, V, L, NT>(values, labels, rows, m, K, p, acc, s);
+    else if (p.rep == NT / 32) e = run_smem<F, V, L, NT / 32>(values, labels, rows, m, K, p, acc, s);
+    else e = run_smem<F, V, L, 1>(values, labels, rows, m, K, p, acc, s);
+  } else {
+    const long long total = rows * K;
+    long long blocks = (total + 255) / 256;
+    if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+    init_global<F, V><<<static_cast<int>(blocks), 256, 0, s>>>(acc, total);
+    dim3 grid(static_cast<unsigned>(p.chunks), static_cast<unsigned>(rows));
+    accum_global<F, V, L, 0><<<grid, NT, 0, s>>>(values, labels, m, K, p.chunk_len, acc);
+    note_launches(2);
+    if (is_select(F)) {
+      accum_global<F, V, L, 1><<<grid, NT, 0, s>>>(values, labels, m, K, p.chunk_len, acc);
+      note_launches(1);
+    }
+  }
+  if (e != cudaSuccess) return kLaunchError;
+  const long long total = rows * K;
+  long long blocks = (total + 255) / 256;
+  if (blocks > num_sms() * 16) blocks = num_sms() * 16;
+  finalize<F, V, O><<<static_cast<int>(blocks), 256, 0, s>>>(acc, values, out, rows, m, K, fold_chunks, ddof);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t nbg_group_workspace_bytes(int func, long long rows, long long m, long long K) {
+  if (func < 0 || func >= kNumFuncs) return 0;
+  return plan_bytes(make_plan(func, rows, m, K), rows, K);
+}
+
+// Exported symbol per (function, values dtype, labels dtype); output dtype follows
+// numbagg: same as values except mean/var/std on integers, which return float64
+// (supports_ints=False, numbagg/decorators.py:614-619).
+#define NBG_GROUP_ONE(NAME, FC, V, VS, O, L, LS)                                               \
+  int nbg_group_##NAME##_##VS##_##LS(const V* values, const L* labels, O* out, long long rows,  \
+                                     long long m, long long num_labels, long long ddof, void* ws, \
+                                     size_t ws_bytes, void* stream) {                          \
+    return launch_group<FC, V, L, O>(values, labels, out, rows, m, num_labels, ddof, ws, ws_bytes, \
+                                     static_cast<cudaStream_t>(stream));                       \
+  }
+#define NBG_GROUP_LABELS(NAME, FC, V, VS, O)    \
+  NBG_GROUP_ONE(NAME, FC, V, VS, O, int, i32) \
+  NBG_GROUP_ONE(NAME, FC, V, VS, O, long long, i64)
+
+#define NBG_GROUP_ALLTYPES(NAME, FC)                 \
+  NBG_GROUP_LABELS(NAME, FC, double, f64, double)    \
+  NBG_GROUP_LABELS(NAME, FC, float, f32, float)      \
+  NBG_GROUP_LABELS(NAME, FC, int, i32, int)          \
+  NBG_GROUP_LABELS(NAME, FC, long long, i64, long long)
+#define NBG_GROUP_FLOATONLY(NAME, FC)                \
+  NBG_GROUP_LABELS(NAME, FC, double, f64, double)    \
+  NBG_GROUP_LABELS(NAME, FC, float, f32, float)
+
+NBG_GROUP_ALLTYPES(nansum, kSum)
+NBG_GROUP_ALLTYPES(nancount, kCount)
+NBG_GROUP_FLOATONLY(nanmean, kMean)
+NBG_GROUP_FLOATONLY(nanvar, kVar)
+NBG_GROUP_FLOATONLY(nanstd, kStd)
+NBG_GROUP_ALLTYPES(nansum_of_squares, kSumSq)
+NBG_GROUP_ALLTYPES(nanargmax, kArgMax)
+NBG_GROUP_ALLTYPES(nanargmin, kArgMin)
+NBG_GROUP_ALLTYPES(nanmax, kMax)
+NBG_GROUP_ALLTYPES(nanmin, kMin)
+NBG_GROUP_ALLTYPES(nanfirst, kFirst)
+NBG_GROUP_ALLTYPES(nanlast, kLast)
+NBG_GROUP_ALLTYPES(nanprod, kProd)
+NBG_GROUP_ALLTYPES(nanany, kAny)
+NBG_GROUP_ALLTYPES(nanall, kAll)
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+"""Exponentially weighted moving functions (numbagg/moving_exp.py), on CUDA.
+
+Same names, keywords and checks as numbagg's ``ndmoveexp`` decorator
+(numbagg/decorators.py:374-414): ``alpha`` is a scalar, a 1-D array along the
+scanned axis, or an array shaped like the input; ``axis`` may be an int or a
+1-tuple, ``axis=()`` returns the input.  alpha and min_weight are rounded to the
+array dtype first, as the gufunc's float32 loop does.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _host, _lib
+
+
+def _move_exp(name: str, arrs, alpha, min_weight, axis):
+    if isinstance(axis, tuple):
+        if axis == ():
+            if len(arrs) > 1:
+                raise ValueError(
+                    "`axis` cannot be an empty tuple when passing more than one array; since we default to returning the input."
+                )
+            return arrs[0]
+        if len(axis) > 1:
+            raise ValueError(f"Only one axis can be passed to {name}; got {axis}")
+        (axis,) = axis
+    shape0 = _host.shape_of(arrs[0])
+    if len(shape0) == 0:
+        raise ValueError(f"{name} requires an array with at least one dimension")
+    axis = _host.normalize_axis(axis, len(shape0))
+    if isinstance(alpha, (np.ndarray, torch.Tensor)) and np.ndim(alpha) == 1 and len(alpha) != shape0[axis]:
+        raise ValueError(f"alpha has length {len(alpha)}, expected {shape0[axis]} (the length of axis {axis})")
+    tensors = []
+    restore = None
+    for x in arrs:
+        t, r = _host.to_device(x)
+        tensors.append(t)
+        restore = restore or r
+    a = tensors[0]
+    dtype = _host.float_compute_dtype(a.dtype)
+    if len(tensors) > 1:
+        tensors = list(torch.broadcast_tensors(*tensors))
+        dtype = _host.float_compute_dtype(torch.promote_types(tensors[0].dtype, tensors[1].dtype))
+    flats = []
+    shape = None
+    for t in tensors:
+        f, shape = _host.rows_last(t.to(dtype), axis)
+        flats.append(f)
+    rows, n = flats[0].shape
+    np_dtype = np.float64 if dtype == torch.float64 else np.float32
+
+    alpha_t = None
+    alpha_scalar = 0.0
+    if isinstance(alpha, (np.ndarray, torch.Tensor)) and np.ndim(alpha) > 0:
+        at, _ = _host.to_device(alpha)
+        at = at.to(device=a.device, dtype=dtype)
+        if at.ndim == 1:
+            if at.shape[0] != n:
+                raise ValueError(f"alpha has length {at.shape[0]}, expected {n} (the length of axis {axis})")
+            alpha_t = at.contiguous()
+            mode = 1
+        else:
+            at = torch.broadcast_to(at, tensors[0].shape)
+            alpha_t, _ = _host.rows_last(at, axis)
+            mode = 2
+    else:
+        alpha_scalar = float(np_dtype(np.asarray(alpha).item() if hasattr(alpha, "shape") else alpha))
+        mode = 0
+    mw = float(np_dtype(min_weight))
+
+    out = torch.empty((rows, n), dtype=dtype, device=a.device)
+    if out.numel():
+        L = _lib.lib()
+        ws = _lib.workspaces.scan(L.nbg_move_exp_workspace_bytes(rows, n), a.device)
+        fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
+        args = [f.data_ptr() for f in flats] + [
+            None if alpha_t is None else alpha_t.data_ptr(),
+            alpha_scalar,
+            mode,
+            mw,
+            out.data_ptr(),
+            rows,
+            n,
+            ws.data_ptr(),
+            ws.numel(),
+            _host.stream(a.device),
+        ]
+        _lib.check(fn(*args), name)
+    return restore(_host.restore_axis(out, shape, axis))
+
+
+def move_exp_nancount(arr, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially decayed count of non-NaN values (numbagg/moving_exp.py:12-38)."""
+    return _move_exp("move_exp_nancount", (arr,), alpha, min_weight, axis)
+
+
+def move_exp_nanmean(arr, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving mean (numbagg/moving_exp.py:41-71)."""
+    return _move_exp("move_exp_nanmean", (arr,), alpha, min_weight, axis)
+
+
+def move_exp_nansum(arr, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving sum (numbagg/moving_exp.py:74-102)."""
+    return _move_exp("move_exp_nansum", (arr,), alpha, min_weight, axis)
+
+
+def move_exp_nanvar(arr, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving variance, bias-corrected (numbagg/moving_exp.py:105-156)."""
+    return _move_exp("move_exp_nanvar", (arr,), alpha, min_weight, axis)
+
+
+def move_exp_nanstd(arr, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving standard deviation (numbagg/moving_exp.py:158-223)."""
+    return _move_exp("move_exp_nanstd", (arr,), alpha, min_weight, axis)
+
+
+def move_exp_nancov(a1, a2, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving covariance (numbagg/moving_exp.py:226-272)."""
+    return _move_exp("move_exp_nancov", (a1, a2), alpha, min_weight, axis)
+
+
+def move_exp_nancorr(a1, a2, /, *, alpha, min_weight=0, axis=-1):
+    """Exponentially weighted moving correlation (numbagg/moving_exp.py:275-335)."""
+    return _move_exp("move_exp_nancorr", (a1, a2), alpha, min_weight, axis)
+
+
+__all__ = [
+    "move_exp_nancorr",
+    "move_exp_nancount",
+    "move_exp_nancov",
+    "move_exp_nanmean",
+    "move_exp_nanstd",
+    "move_exp_nansum",
+    "move_exp_nanvar",
+]

@@ -1,0 +1,171 @@
+"""Comparison helpers for the GPU parity tests.
+
+Floating-point results are compared with a scaled relative error
+    err = |gpu - ref| / max(|ref|, S)
+where S is the natural magnitude of the statistic at that position (the window sum
+of |x| for a sum, the window mean of x^2 for a variance, 1 for a correlation...).
+A plain relative error is meaningless where the statistic itself cancels to ~0: the
+reference's own running sums carry rounding residue there.
+
+NaN placement must agree exactly, except at positions where the reference's value is
+itself rounding noise of a mathematically degenerate quantity; callers pass those as
+`allow` (see the masks below).  The fraction of allowed positions is reported by the
+tests and must stay small.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+import oracle
+
+F64_TOL = 1e-12
+F32_TOL = 2e-6
+
+
+def scaled_error(got, ref, scale, allow=None):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.broadcast_to(np.asarray(scale, dtype=np.float64), ref.shape)
+    gn, rn = np.isnan(got), np.isnan(ref)
+    allow = np.zeros(ref.shape, bool) if allow is None else np.asarray(allow, bool)
+    nan_bad = (gn != rn) & ~allow
+    both = ~gn & ~rn & ~allow
+    inf = both & (np.isinf(ref) | np.isinf(got))
+    inf_bad = inf & (got != ref)
+    fin = both & ~inf
+    denom = np.fmax(np.abs(ref[fin]), np.abs(scale[fin]))
+    diff = np.abs(got[fin] - ref[fin])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        err = np.where(denom > 0, diff / np.where(denom > 0, denom, 1), diff)
+    return {
+        "nan_mismatch": int(nan_bad.sum()),
+        "inf_mismatch": int(inf_bad.sum()),
+        "max_err": float(err.max()) if err.size else 0.0,
+        "allowed": int(allow.sum()),
+        "n": int(ref.size),
+    }
+
+
+def assert_scaled_close(got, ref, scale, tol, allow=None, what=""):
+    r = scaled_error(got, ref, scale, allow)
+    assert r["nan_mismatch"] == 0, f"{what}: NaN placement differs at {r['nan_mismatch']} positions ({r})"
+    assert r["inf_mismatch"] == 0, f"{what}: inf differs ({r})"
+    assert r["max_err"] <= tol, f"{what}: scaled error {r['max_err']:.3g} > {tol:g} ({r})"
+    return r
+
+
+def assert_bit_equal(got, ref, what=""):
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    assert got.shape == ref.shape and got.dtype == ref.dtype, f"{what}: {got.shape}/{got.dtype} vs {ref.shape}/{ref.dtype}"
+    if got.dtype.kind == "f":
+        gn, rn = np.isnan(got), np.isnan(ref)
+        assert np.array_equal(gn, rn), f"{what}: NaN placement differs"
+        keep = ~gn
+        assert np.array_equal(got[keep], ref[keep]), f"{what}: values differ"
+        assert np.array_equal(np.signbit(got[keep]), np.signbit(ref[keep])), f"{what}: signed zeros differ"
+    else:
+        assert np.array_equal(got, ref), f"{what}: values differ"
+
+
+# ---- scales -------------------------------------------------------------------------
+
+
+def _cond(msq, var):
+    """mean(x^2) / var(x): how much a rounding residue in the running sums is
+    amplified in a variance-normalised result."""
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(var > 0, msq / np.where(var > 0, var, 1.0), np.inf)
+
+
+def move_scale(name, a, b, window, axis=-1):
+    absa = np.abs(np.asarray(a, dtype=np.float64))
+    if name == "move_sum":
+        return oracle.move("move_sum", absa, window=window, min_count=0, axis=axis)
+    if name == "move_mean":
+        return oracle.move("move_mean", absa, window=window, min_count=1, axis=axis)
+    sq = oracle.move("move_mean", absa * absa, window=window, min_count=1, axis=axis)
+    if name == "move_var":
+        return sq
+    if name == "move_std":
+        std = oracle.move("move_std", np.asarray(a, dtype=np.float64), window=window, min_count=2, axis=axis)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.fmax(np.sqrt(sq), sq / std)
+    absb = np.abs(np.asarray(b, dtype=np.float64))
+    sqb = oracle.move("move_mean", absb * absb, window=window, min_count=1, axis=axis)
+    if name == "move_cov":
+        return np.sqrt(sq * sqb)
+    # move_corr
+    va = oracle.move("move_var", np.asarray(a, dtype=np.float64), window=window, min_count=2, axis=axis)
+    vb = oracle.move("move_var", np.asarray(b, dtype=np.float64), window=window, min_count=2, axis=axis)
+    return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)))
+
+
+def exp_scale(name, a, b, alpha, axis=-1):
+    a64 = np.asarray(a, dtype=np.float64)
+    absa = np.abs(a64)
+    if name == "move_exp_nancount":
+        return np.ones_like(absa)
+    al = alpha if not isinstance(alpha, np.ndarray) else alpha.astype(np.float64)
+    if name == "move_exp_nansum":
+        return oracle.move_exp("move_exp_nansum", absa, alpha=al, axis=axis)
+    if name == "move_exp_nanmean":
+        return oracle.move_exp("move_exp_nanmean", absa, alpha=al, axis=axis)
+    sq = oracle.move_exp("move_exp_nanmean", absa * absa, alpha=al, axis=axis)
+    if name == "move_exp_nanvar":
+        return sq
+    if name == "move_exp_nanstd":
+        std = oracle.move_exp("move_exp_nanstd", a64, alpha=al, axis=axis)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.fmax(np.sqrt(sq), sq / std)
+    b64 = np.asarray(b, dtype=np.float64)
+    absb = np.abs(b64)
+    sqb = oracle.move_exp("move_exp_nanmean", absb * absb, alpha=al, axis=axis)
+    if name == "move_exp_nancov":
+        return np.sqrt(sq * sqb)
+    va = oracle.move_exp("move_exp_nanvar", a64, alpha=al, axis=axis)
+    vb = oracle.move_exp("move_exp_nanvar", b64, alpha=al, axis=axis)
+    return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)))
+
+
+# ---- degenerate positions ---------------------------------------------------------------
+
+
+def _valid(a, b):
+    v = ~np.isnan(np.asarray(a, dtype=np.float64))
+    if b is not None:
+        v &= ~np.isnan(np.asarray(b, dtype=np.float64))
+    return v
+
+
+def move_degenerate(name, a, b, window, axis=-1):
+    """move_corr over a window holding a single pair: both variances are 0
+    mathematically, the reference's value is the sign of its rounding residue."""
+    if name != "move_corr":
+        return None
+    v = _valid(a, b).astype(np.float64)
+    cnt = oracle.move("move_sum", v, window=window, min_count=0, axis=axis)
+    return cnt <= 1.5
+
+
+def exp_degenerate(name, a, b, alpha, min_weight, axis=-1):
+    """Positions where the reference's decision rests on rounding noise:
+    * variance-like functions while at most one observation has been seen (bias is 0
+      mathematically; the reference compares its rounding residue with 0);
+    * any function where the running weight equals min_weight to ~1e-12."""
+    v = _valid(a, b)
+    allow = np.zeros(v.shape, bool)
+    if name in ("move_exp_nanvar", "move_exp_nanstd", "move_exp_nancov", "move_exp_nancorr"):
+        seen = np.cumsum(np.moveaxis(v, axis, -1), axis=-1)
+        allow |= np.moveaxis(seen <= 1, -1, axis)
+    al = alpha if not isinstance(alpha, np.ndarray) else alpha.astype(np.float64)
+    if isinstance(al, np.ndarray) and al.ndim == 1:
+        al_full = np.broadcast_to(np.moveaxis(np.broadcast_to(al, np.moveaxis(v, axis, -1).shape), -1, axis), v.shape)
+    else:
+        al_full = np.broadcast_to(al, v.shape)
+    w_in = np.where(v, al_full, np.nan)
+    weight = oracle.move_exp("move_exp_nansum", w_in, alpha=al, axis=axis)
+    weight = np.where(np.isnan(weight), 0.0, weight)
+    allow |= np.abs(weight - min_weight) <= 1e-12 * max(1.0, abs(min_weight))
+    return allow
