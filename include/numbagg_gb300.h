@@ -8,13 +8,14 @@
  * device pointers for data, `stream` is a cudaStream_t (NULL = legacy default).
  * Calls are asynchronous on `stream`; every call returns an NBG_* status.
  *
- * Workspaces.  Scans along a row (moving windows, exponential moving functions,
- * fills) carry state between tiles through a workspace sized by the matching
- * *_workspace_bytes() query.  A scan workspace must be zero-filled once when it is
- * allocated; it then maintains itself across launches.  One workspace per stream:
- * launches that share a workspace must be ordered on one stream.  Grouped
- * reductions take a scratch buffer sized by nbg_group_workspace_bytes() that needs
- * no initialisation (do not share it with a scan workspace).
+ * Workspaces.  Moving windows and fills carry state between tiles through a
+ * look-back workspace sized by nbg_move_workspace_bytes() / nbg_fill_workspace_bytes().
+ * A look-back workspace must be zero-filled once when it is allocated; it then
+ * maintains itself across launches.  One workspace per stream: launches that share
+ * it must be ordered on one stream.  The exponential moving functions and the grouped
+ * reductions take a scratch buffer (nbg_move_exp_workspace_bytes(),
+ * nbg_group_workspace_bytes()) that needs no initialisation; do not share a scratch
+ * buffer with a look-back workspace.
  */
 #ifndef NUMBAGG_GB300_H
 #define NUMBAGG_GB300_H
@@ -82,6 +83,7 @@ NBG_DECL_MOVE2(move_corr, float, f32)
  *   move_exp_nansum   numbagg/moving_exp.py:74-102   move_exp_nanvar  numbagg/moving_exp.py:105-156
  *   move_exp_nanstd   numbagg/moving_exp.py:158-223  move_exp_nancov  numbagg/moving_exp.py:226-272
  *   move_exp_nancorr  numbagg/moving_exp.py:275-335
+ * ws: scratch (no initialisation), nbg_move_exp_workspace_bytes() bytes.
  * alpha_mode 0: scalar alpha_scalar (already rounded to the array dtype);
  * 1: `alpha` holds n values shared by every row; 2: `alpha` holds rows x n values.
  * min_weight is the array-dtype value widened to double. */

@@ -6,12 +6,15 @@
 // value is NaN); sum_weight_2 decays by decay_i**2.  A position is therefore an
 // affine map s -> A*s + B, and maps compose associatively:
 //     (A2, B2) o (A1, B1) = (A2*A1, A2*B1 + B2).
-// A row is cut into tiles; each thread composes the maps of its K positions, a
-// warp-shuffle scan composes threads, and the map of everything before a tile comes
-// from a decoupled look-back (an inclusive prefix is published as the constant map
-// A = 0, B = state).  The second pass replays each position with the reference's
-// own update, a rounded multiply followed by a rounded add (no FMA), starting from
-// the carried state, and finalises with the reference's formulas.
+// A row is cut into tiles.  Phase 0 composes each tile's map (thread-serial over K
+// positions, then a fixed-structure warp-shuffle scan); phase 1 scans the tile maps
+// of each row in a fixed order to get the state entering every tile; phase 2 replays
+// each position with the reference's own update, a rounded multiply followed by a
+// rounded add (no FMA), starting from that state, and finalises with the reference's
+// formulas.  The composition order never depends on timing, so results are
+// bit-identical run to run and a prefix of a row gives the same bits as the whole
+// row.  Phase 0 and 2 both read the input; the plain float64 form is bound by the
+// FP64 pipe (about 1.6 adds per clock per SM on GB300), not by that extra read.
 //
 // alpha: a scalar, a 1-D array along the scanned axis shared by every row, or one
 // value per element (numbagg/decorators.py:398-409).
@@ -153,69 +156,133 @@ NBG_DEVICE double finalize(const double* s, int seen, double min_weight) {
 
 constexpr int NT = 128;
 
-template <int OP, typename T, int K>
-__global__ void __launch_bounds__(NT) exp_kernel(const T* __restrict__ a, const T* __restrict__ b,
-                                                 const T* __restrict__ alpha_arr, double alpha_scalar,
-                                                 int alpha_mode, double min_weight,
-                                                 T* __restrict__ out, long long rows, long long n,
-                                                 long long tiles_per_row, void* ws_base,
-                                                 size_t ws_bytes) {
+// Phase 0 (PHASE == 0): the map of each tile, composed in position order, to maps[].
+// Phase 2 (PHASE == 2): outputs, starting from the state carries[tile] before the tile.
+// One CTA per tile; tiles do not wait on each other.
+template <int OP, typename T, int K, int PHASE>
+__global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                      const T* __restrict__ alpha_arr, double alpha_scalar,
+                                                      int alpha_mode, double min_weight,
+                                                      T* __restrict__ out, long long rows, long long n,
+                                                      long long tiles_per_row, Map<Traits<OP>::NS>* maps,
+                                                      const Map<Traits<OP>::NS>* carries) {
   constexpr int NS = Traits<OP>::NS;
   constexpr long long TILE = static_cast<long long>(NT) * K;
   using M = Map<NS>;
   __shared__ M warp_tot[NT / 32];
-  __shared__ M carry_smem;
-  __shared__ long long tile_smem;
-  const long long total_tiles = rows * tiles_per_row;
-  Workspace ws = make_workspace(ws_base, ws_bytes);
-  const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long tile = blockIdx.x;
+  const long long row = tile / tiles_per_row;
+  const long long chunk = tile - row * tiles_per_row;
+  const long long p0 = chunk * TILE + static_cast<long long>(threadIdx.x) * K;
+  const T* ar = a + row * n;
+  const T* br = Traits<OP>::TWO ? b + row * n : nullptr;
+  const T* alr = alpha_mode == 2 ? alpha_arr + row * n : alpha_arr;
 
-  for (;;) {
-    if (threadIdx.x == 0) tile_smem = claim_tile(ws.hdr);
-    __syncthreads();
-    const long long tile = tile_smem;
-    if (tile >= total_tiles) break;
-    const TileCoord tc = tile_coord(tile, rows);
-    const long long row = tc.row, chunk = tc.chunk;
-    const long long p0 = chunk * TILE + static_cast<long long>(threadIdx.x) * K;
-    const T* ar = a + row * n;
-    const T* br = Traits<OP>::TWO ? b + row * n : nullptr;
-    const T* alr = alpha_mode == 2 ? alpha_arr + row * n : alpha_arr;
-
-    T xv[K], yv[K];
-    double al[K];
+  T xv[K], yv[K];
+  double al[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      const bool in = i < n;
-      xv[k] = in ? ar[i] : T(0);
-      yv[k] = (Traits<OP>::TWO && in) ? br[i] : T(0);
-      al[k] = alpha_mode == 0 ? alpha_scalar : (in ? static_cast<double>(alr[i]) : 0.0);
+  for (int k = 0; k < K; ++k) {
+    const long long i = p0 + k;
+    const bool in = i < n;
+    xv[k] = in ? ar[i] : T(0);
+    yv[k] = (Traits<OP>::TWO && in) ? br[i] : T(0);
+    al[k] = alpha_mode == 0 ? alpha_scalar : (in ? static_cast<double>(alr[i]) : 0.0);
+  }
+  // ---- this thread's maps composed in order ----
+  M agg = identity_map<OP>();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const long long i = p0 + k;
+    if (i >= n) break;
+    const double d = __dadd_rn(1.0, -al[k]);
+    const double dd = __dmul_rn(d, d);
+    bool valid = !is_nan(xv[k]);
+    if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
+    double bj[NS];
+    contributions<OP>(static_cast<double>(xv[k]), static_cast<double>(yv[k]), al[k], bj);
+    agg.A1 = agg.A1 * d;
+    agg.A2 = agg.A2 * dd;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const double f = (j == Traits<OP>::W2) ? dd : d;
+      agg.B[j] = valid ? fma(agg.B[j], f, bj[j]) : agg.B[j] * f;
     }
-    // ---- pass 1: compose this thread's maps ----
-    M agg = identity_map<OP>();
+    agg.seen |= valid ? 1 : 0;
+  }
+  // ---- block scan (fixed structure, so the result does not depend on timing) ----
+  M incl = agg;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      if (i >= n) break;
-      const double d = __dadd_rn(1.0, -al[k]);
-      const double dd = __dmul_rn(d, d);
-      bool valid = !is_nan(xv[k]);
-      if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
+  for (int dlt = 1; dlt < 32; dlt <<= 1) {
+    const M up = shfl_up_map<OP>(incl, dlt);
+    if (lane >= dlt) incl = compose<OP>(up, incl);
+  }
+  M excl = shfl_up_map<OP>(incl, 1);
+  if (lane == 0) excl = identity_map<OP>();
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    M run = warp_tot[0];
+    for (int w = 1; w < NT / 32; ++w) {
+      run = compose<OP>(run, warp_tot[w]);
+      warp_tot[w] = run;
+    }
+  }
+  __syncthreads();
+  if (PHASE == 0) {
+    if (threadIdx.x == 0) maps[tile] = warp_tot[NT / 32 - 1];
+    return;
+  }
+  if (warp > 0) excl = compose<OP>(warp_tot[warp - 1], excl);
+  // state entering this thread = (excl o carry) applied to the zero state
+  const M start = compose<OP>(carries[tile], excl);
+  double s[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) s[j] = start.B[j];
+  int seen = start.seen;
+
+  // ---- the reference's update, position by position ----
+  T* orow = out + row * n;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const long long i = p0 + k;
+    if (i >= n) break;
+    const double d = __dadd_rn(1.0, -al[k]);
+    const double dd = __dmul_rn(d, d);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) s[j] = __dmul_rn(s[j], (j == Traits<OP>::W2) ? dd : d);
+    bool valid = !is_nan(xv[k]);
+    if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
+    if (valid) {
       double bj[NS];
       contributions<OP>(static_cast<double>(xv[k]), static_cast<double>(yv[k]), al[k], bj);
-      agg.A1 = agg.A1 * d;
-      agg.A2 = agg.A2 * dd;
 #pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        const double f = (j == Traits<OP>::W2) ? dd : d;
-        agg.B[j] = valid ? fma(agg.B[j], f, bj[j]) : agg.B[j] * f;
-      }
-      agg.seen |= valid ? 1 : 0;
+      for (int j = 0; j < NS; ++j) s[j] = __dadd_rn(s[j], bj[j]);
+      seen = 1;
     }
-    // ---- block scan (exclusive) of the thread maps ----
-    M incl = agg;
+    orow[i] = static_cast<T>(finalize<OP>(s, seen, min_weight));
+  }
+}
+
+// Phase 1: per row, the state before each tile, composing the tile maps in a fixed
+// order (a block-wide scan over chunks of NT tiles), so the carries are reproducible.
+template <int OP>
+__global__ void __launch_bounds__(NT) exp_carry_kernel(const Map<Traits<OP>::NS>* __restrict__ maps,
+                                                       Map<Traits<OP>::NS>* __restrict__ carries,
+                                                       long long tiles_per_row) {
+  using M = Map<Traits<OP>::NS>;
+  __shared__ M warp_tot[NT / 32];
+  __shared__ M running_smem;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long row = blockIdx.x;
+  const M* mr = maps + row * tiles_per_row;
+  M* cr = carries + row * tiles_per_row;
+  if (threadIdx.x == 0) running_smem = identity_map<OP>();
+  __syncthreads();
+  for (long long base = 0; base < tiles_per_row; base += NT) {
+    const long long t = base + threadIdx.x;
+    M v = t < tiles_per_row ? mr[t] : identity_map<OP>();
+    M incl = v;
 #pragma unroll
     for (int dlt = 1; dlt < 32; dlt <<= 1) {
       const M up = shfl_up_map<OP>(incl, dlt);
@@ -229,69 +296,22 @@ __global__ void __launch_bounds__(NT) exp_kernel(const T* __restrict__ a, const 
       M run = warp_tot[0];
       for (int w = 1; w < NT / 32; ++w) {
         run = compose<OP>(run, warp_tot[w]);
-        warp_tot[w] = run;  // inclusive over warps 0..w
+        warp_tot[w] = run;
       }
     }
     __syncthreads();
     if (warp > 0) excl = compose<OP>(warp_tot[warp - 1], excl);
-    if (warp == 0) {
-      const M tile_map = warp_tot[NT / 32 - 1];
-      if (chunk == 0) {
-        if (lane == 0) {
-          if (tiles_per_row > 1) {
-            M pre = tile_map;
-            pre.A1 = 0.0;
-            pre.A2 = 0.0;
-            publish(ws, tile, epoch, kStatePrefix, pre);
-          }
-          carry_smem = identity_map<OP>();
-        }
-      } else {
-        if (lane == 0) publish(ws, tile, epoch, kStateAggregate, tile_map);
-        __syncwarp();
-        bool ok;
-        const M carry = warp_lookback<M>(ws, tile, chunk, rows, epoch, ComposeOp<OP>(), ok);
-        if (lane == 0) {
-          M pre = compose<OP>(carry, tile_map);
-          pre.A1 = 0.0;
-          pre.A2 = 0.0;
-          publish(ws, tile, epoch, kStatePrefix, pre);
-          carry_smem = carry;
-        }
-      }
+    const M running = running_smem;
+    if (t < tiles_per_row) {
+      M c = compose<OP>(running, excl);
+      c.A1 = 0.0;  // only the state (B) is used downstream
+      c.A2 = 0.0;
+      cr[t] = c;
     }
     __syncthreads();
-    // state entering this thread = (excl o carry) applied to the zero state
-    const M start = compose<OP>(carry_smem, excl);
-    double s[NS];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) s[j] = start.B[j];
-    int seen = start.seen;
-
-    // ---- pass 2: the reference's update, position by position ----
-    T* orow = out + row * n;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      if (i >= n) break;
-      const double d = __dadd_rn(1.0, -al[k]);
-      const double dd = __dmul_rn(d, d);
-#pragma unroll
-      for (int j = 0; j < NS; ++j) s[j] = __dmul_rn(s[j], (j == Traits<OP>::W2) ? dd : d);
-      bool valid = !is_nan(xv[k]);
-      if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
-      if (valid) {
-        double bj[NS];
-        contributions<OP>(static_cast<double>(xv[k]), static_cast<double>(yv[k]), al[k], bj);
-#pragma unroll
-        for (int j = 0; j < NS; ++j) s[j] = __dadd_rn(s[j], bj[j]);
-        seen = 1;
-      }
-      orow[i] = static_cast<T>(finalize<OP>(s, seen, min_weight));
-    }
+    if (threadIdx.x == 0) running_smem = compose<OP>(running, warp_tot[NT / 32 - 1]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) finish_cta(ws.hdr);
 }
 
 }  // namespace mexp
@@ -308,6 +328,11 @@ long long exp_tiles_per_row(long long n) {
   return n <= 0 ? 0 : (n + tile - 1) / tile;
 }
 
+template <int OP>
+size_t exp_scratch_bytes(long long rows, long long n) {
+  return 2 * static_cast<size_t>(rows * exp_tiles_per_row(n)) * sizeof(Map<Traits<OP>::NS>) + 256;
+}
+
 template <int OP, typename T>
 int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int alpha_mode,
                double min_weight, T* out, long long rows, long long n, void* ws, size_t ws_bytes,
@@ -317,23 +342,27 @@ int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int 
   if (!a || !out || (Traits<OP>::TWO && !b) || (alpha_mode > 0 && !alpha)) return kInvalidArgument;
   const long long tpr = exp_tiles_per_row(n);
   const long long total = rows * tpr;
-  if (!ws || ws_bytes < workspace_bytes(total)) return kWorkspaceTooSmall;
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long cap = static_cast<long long>(sms) * 12;
-  const int grid = static_cast<int>(total < cap ? total : cap);
-  exp_kernel<OP, T, kExpK><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out,
-                                                rows, n, tpr, ws, ws_bytes);
-  note_launches(1);
+  if (total > 0x7fffffffll) return kUnsupported;
+  if (!ws || ws_bytes < exp_scratch_bytes<OP>(rows, n)) return kWorkspaceTooSmall;
+  using M = Map<Traits<OP>::NS>;
+  M* maps = reinterpret_cast<M*>((reinterpret_cast<size_t>(ws) + 127) & ~static_cast<size_t>(127));
+  M* carries = maps + total;
+  const int grid = static_cast<int>(total);
+  exp_tile_kernel<OP, T, kExpK, 0><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight,
+                                                       out, rows, n, tpr, maps, carries);
+  exp_carry_kernel<OP><<<static_cast<int>(rows), NT, 0, s>>>(maps, carries, tpr);
+  exp_tile_kernel<OP, T, kExpK, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight,
+                                                       out, rows, n, tpr, maps, carries);
+  note_launches(3);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 }  // namespace
 
 extern "C" {
 
+// the largest state (move_exp_nancorr) bounds every function's scratch
 size_t nbg_move_exp_workspace_bytes(long long rows, long long n) {
-  return workspace_bytes(rows * exp_tiles_per_row(n));
+  return exp_scratch_bytes<kCorr>(rows, n);
 }
 
 // alpha_mode: 0 = scalar `alpha_scalar`, 1 = `alpha` has n values shared by all rows,

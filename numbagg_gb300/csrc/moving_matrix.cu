@@ -21,7 +21,7 @@ constexpr int NT = 256;
 constexpr int kRcp = 1024;
 
 NBG_DEVICE double div_count(double s, long long c, const double* rcp) {
-  if (c < kRcp) {
+  if (c < kRcp && isfinite(s)) {
     const double r = rcp[c];
     const double q0 = s * r;
     const double e = fma(-q0, static_cast<double>(c), s);

@@ -91,7 +91,11 @@ struct WsHeader {
 };
 static_assert(sizeof(WsHeader) == 256, "header must stay 256 bytes");
 
-constexpr int kPayloadBytes = 128;  // per-tile look-back payload slot
+// Each tile has two payload slots, one for its aggregate and one for its inclusive
+// prefix, each written once per launch: a reader that saw "aggregate" must never
+// find the slot rewritten under it by the later prefix.
+constexpr int kPayloadBytes = 128;  // per slot
+constexpr int kSlotsPerTile = 2;
 constexpr unsigned kStateNone = 0, kStateAggregate = 1, kStatePrefix = 2;
 
 struct Workspace {
@@ -101,7 +105,7 @@ struct Workspace {
 };
 
 NBG_HOST_DEVICE size_t workspace_bytes(long long tiles) {
-  return 256 + static_cast<size_t>(tiles) * (8 + kPayloadBytes) + 256;
+  return 256 + static_cast<size_t>(tiles) * (8 + kSlotsPerTile * kPayloadBytes) + 256;
 }
 
 // The layout depends only on the workspace size, so every kernel that shares a
@@ -109,7 +113,7 @@ NBG_HOST_DEVICE size_t workspace_bytes(long long tiles) {
 NBG_HOST_DEVICE Workspace make_workspace(void* base, size_t bytes) {
   Workspace w;
   unsigned char* p = static_cast<unsigned char*>(base);
-  const size_t cap = bytes > 512 ? (bytes - 512) / (8 + kPayloadBytes) : 0;
+  const size_t cap = bytes > 512 ? (bytes - 512) / (8 + kSlotsPerTile * kPayloadBytes) : 0;
   w.hdr = reinterpret_cast<WsHeader*>(p);
   w.status = reinterpret_cast<unsigned long long*>(p + 256);
   size_t off = 256 + cap * 8;
@@ -159,11 +163,15 @@ NBG_DEVICE unsigned long long status_word(unsigned epoch, unsigned state) {
   return (static_cast<unsigned long long>(epoch) << 8) | 0xA0ull | state;
 }
 
+NBG_DEVICE unsigned char* payload_slot(const Workspace& ws, long long tile, unsigned state) {
+  return ws.payload + (static_cast<size_t>(tile) * kSlotsPerTile + (state == kStatePrefix ? 1 : 0)) * kPayloadBytes;
+}
+
 template <typename P>
 NBG_DEVICE void publish(const Workspace& ws, long long tile, unsigned epoch, unsigned state,
                         const P& value) {
   static_assert(sizeof(P) <= kPayloadBytes, "payload too large");
-  P* slot = reinterpret_cast<P*>(ws.payload + static_cast<size_t>(tile) * kPayloadBytes);
+  P* slot = reinterpret_cast<P*>(payload_slot(ws, tile, state));
   *slot = value;
   __threadfence();
   atomicExch(ws.status + tile, status_word(epoch, state));
@@ -190,9 +198,8 @@ NBG_DEVICE unsigned wait_status(const Workspace& ws, long long tile, unsigned ep
 }
 
 template <typename P>
-NBG_DEVICE P read_payload(const Workspace& ws, long long tile) {
-  const volatile unsigned* src =
-      reinterpret_cast<const volatile unsigned*>(ws.payload + static_cast<size_t>(tile) * kPayloadBytes);
+NBG_DEVICE P read_payload(const Workspace& ws, long long tile, unsigned state) {
+  const volatile unsigned* src = reinterpret_cast<const volatile unsigned*>(payload_slot(ws, tile, state));
   P v;
   // copy through volatile words so the compiler cannot hoist the load above the wait
   unsigned* dst = reinterpret_cast<unsigned*>(&v);
@@ -242,7 +249,7 @@ NBG_DEVICE P warp_lookback(const Workspace& ws, long long tile, long long chunk,
     if (lane < n) {
       const long long p = tile - stride * (done + 1 + lane);
       st = wait_status(ws, p, epoch);
-      if (st != kStateNone) v = read_payload<P>(ws, p);
+      if (st != kStateNone) v = read_payload<P>(ws, p, st);
     }
     if (__ballot_sync(0xffffffffu, lane < n && st == kStateNone)) {
       if (lane == 0) record_error(ws.hdr, kLookbackTimeout, static_cast<unsigned>(tile));

@@ -73,7 +73,7 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis):
     out = torch.empty((rows, n), dtype=dtype, device=a.device)
     if out.numel():
         L = _lib.lib()
-        ws = _lib.workspaces.scan(L.nbg_move_exp_workspace_bytes(rows, n), a.device)
+        ws = _lib.workspaces.scratch(L.nbg_move_exp_workspace_bytes(rows, n), a.device)
         fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
         args = [f.data_ptr() for f in flats] + [
             None if alpha_t is None else alpha_t.data_ptr(),

@@ -95,8 +95,11 @@ def _restore(flat: np.ndarray, shape: tuple[int, ...], axis: int) -> np.ndarray:
     return np.moveaxis(flat.reshape(shape), -1, axis)
 
 
-def move(name, a, b=None, *, window, min_count=None, axis=-1, nthreads=0):
-    """numbagg.move_* restated (ndmove.__call__, numbagg/decorators.py:305-341)."""
+def move(name, a, b=None, *, window, min_count=None, axis=-1, nthreads=0, ext=False):
+    """numbagg.move_* restated (ndmove.__call__, numbagg/decorators.py:305-341).
+
+    ext=True runs the same loop with long double accumulators (IEEE binary128 on
+    aarch64, 80-bit on x86-64): an estimate of the exact result."""
     a = np.asarray(a)
     if min_count is None:
         min_count = window
@@ -108,7 +111,7 @@ def move(name, a, b=None, *, window, min_count=None, axis=-1, nthreads=0):
     fa, shape = _rows_last(a.astype(a.dtype.newbyteorder("="), copy=False), axis)
     out = np.empty_like(fa)
     rows, n = fa.shape
-    fn = getattr(lib(), f"orc_{name}_{dt}")
+    fn = getattr(lib(), f"orc_{name}_ext_{dt}" if ext else f"orc_{name}_{dt}")
     if name in MOVE2:
         fb, _ = _rows_last(np.asarray(b).astype(fa.dtype), axis)
         fn(_p(fa), _p(fb), _p(out), _i(rows), _i(n), _i(window), _i(min_count), ctypes.c_int(nthreads))
@@ -117,8 +120,9 @@ def move(name, a, b=None, *, window, min_count=None, axis=-1, nthreads=0):
     return _restore(out, shape, axis)
 
 
-def move_exp(name, a, b=None, *, alpha, min_weight=0.0, axis=-1, nthreads=0):
-    """numbagg.move_exp_* restated (ndmoveexp.__call__, numbagg/decorators.py:374-414)."""
+def move_exp(name, a, b=None, *, alpha, min_weight=0.0, axis=-1, nthreads=0, ext=False):
+    """numbagg.move_exp_* restated (ndmoveexp.__call__, numbagg/decorators.py:374-414).
+    ext=True: long double accumulators, as for move()."""
     a = np.asarray(a)
     dtype = np.dtype(a.dtype).newbyteorder("=")
     dt = _F[dtype]
@@ -135,7 +139,7 @@ def move_exp(name, a, b=None, *, alpha, min_weight=0.0, axis=-1, nthreads=0):
         stride = n
     out = np.empty_like(fa)
     mw = ctypes.c_double(min_weight) if dt == "f64" else ctypes.c_float(min_weight)
-    fn = getattr(lib(), f"orc_{name}_{dt}")
+    fn = getattr(lib(), f"orc_{name}_ext_{dt}" if ext else f"orc_{name}_{dt}")
     if name in MOVE_EXP2:
         fb, _ = _rows_last(np.asarray(b).astype(dtype), axis)
         fn(_p(fa), _p(fb), _p(al), _i(stride), mw, _p(out), _i(rows), _i(n), ctypes.c_int(nthreads))
@@ -206,9 +210,10 @@ def group(name, values, labels, *, num_labels=None, axis=None, ddof=1, nthreads=
     return out.reshape(bshape + (num_labels,))
 
 
-def move_matrix(name, a, *, window, min_count=None, nthreads=0):
+def move_matrix(name, a, *, window, min_count=None, nthreads=0, ext=False):
     """numbagg.move_covmatrix / move_corrmatrix restated (ndmovematrix.__call__,
-    numbagg/decorators.py:778-807)."""
+    numbagg/decorators.py:778-807).  ext=True computes in long double (arrays and
+    accumulators) and returns float64."""
     a = np.asarray(a)
     if a.ndim < 2:
         raise ValueError(f"{name} requires at least a 2D array with shape (..., obs, vars).")
@@ -220,6 +225,8 @@ def move_matrix(name, a, *, window, min_count=None, nthreads=0):
         raise ValueError(f"window not in valid range: {window}")
     dtype = np.dtype(a.dtype).newbyteorder("=")
     dt = _F[dtype]
+    if ext:
+        dtype, dt = np.dtype(np.longdouble), "ld"
     t_obs, n_vars = a.shape[-2:]
     fa = np.ascontiguousarray(a.astype(dtype, copy=False)).reshape(-1, t_obs, n_vars)
     out = np.empty((fa.shape[0], t_obs, n_vars, n_vars), dtype=dtype)
@@ -227,6 +234,8 @@ def move_matrix(name, a, *, window, min_count=None, nthreads=0):
         _p(fa), _p(out), _i(fa.shape[0]), _i(t_obs), _i(n_vars), _i(window), _i(min_count),
         ctypes.c_int(nthreads),
     )
+    if ext:
+        out = out.astype(np.float64)
     return out.reshape(a.shape[:-2] + (t_obs, n_vars, n_vars))
 
 

@@ -17,7 +17,8 @@ LIB = os.path.join(HERE, "libnbg_oracle.so")
 
 
 def build(force: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "scan_loops.inc")))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [

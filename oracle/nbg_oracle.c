@@ -46,347 +46,24 @@ static int orc_threads(int nthreads) {
 #define INT_NAN_i64 INT64_MIN
 
 /* ------------------------------------------------------------------------------ */
-/* Moving windows: numbagg/moving.py                                               */
+/* Moving windows and exponentially weighted functions (scan_loops.inc)            */
 /* ------------------------------------------------------------------------------ */
 
-/* move_mean, numbagg/moving.py:12-55 */
-#define DEF_MOVE_MEAN(T, SFX)                                                         \
-  EXPORT int orc_move_mean_##SFX(const T* a_, T* out_, int64_t rows, int64_t n,        \
-                                 int64_t window, int64_t min_count, int nthreads) {    \
-    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
-    for (int64_t r = 0; r < rows; ++r) {                                               \
-      const T* a = a_ + r * n; T* out = out_ + r * n;                                  \
-      double asum = 0.0; int64_t count = 0;                                            \
-      int64_t mc = min_count > 1 ? min_count : 1;                                      \
-      int64_t w0 = window < n ? window : n;                                            \
-      for (int64_t i = 0; i < w0; ++i) {                                               \
-        double ai = (double)a[i];                                                      \
-        if (!isnan(ai)) { asum += ai; count += 1; }                                    \
-        out[i] = (T)(count >= mc ? asum / (double)count : NAN);                        \
-      }                                                                                \
-      for (int64_t i = window; i < n; ++i) {                                           \
-        double ai = (double)a[i]; double aold = (double)a[i - window];                 \
-        if (!isnan(aold)) { asum -= aold; count -= 1; }                                \
-        if (!isnan(ai)) { asum += ai; count += 1; }                                    \
-        out[i] = (T)(count >= mc ? asum / (double)count : NAN);                        \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_sum, numbagg/moving.py:58-99 (adds the new value before removing the old) */
-#define DEF_MOVE_SUM(T, SFX)                                                          \
-  EXPORT int orc_move_sum_##SFX(const T* a_, T* out_, int64_t rows, int64_t n,         \
-                                int64_t window, int64_t min_count, int nthreads) {     \
-    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
-    for (int64_t r = 0; r < rows; ++r) {                                               \
-      const T* a = a_ + r * n; T* out = out_ + r * n;                                  \
-      double asum = 0.0; int64_t count = 0;                                            \
-      int64_t w0 = window < n ? window : n;                                            \
-      for (int64_t i = 0; i < w0; ++i) {                                               \
-        double ai = (double)a[i];                                                      \
-        if (!isnan(ai)) { asum += ai; count += 1; }                                    \
-        out[i] = (T)(count >= min_count ? asum : NAN);                                 \
-      }                                                                                \
-      for (int64_t i = window; i < n; ++i) {                                           \
-        double ai = (double)a[i]; double aold = (double)a[i - window];                 \
-        if (!isnan(ai)) { asum += ai; count += 1; }                                    \
-        if (!isnan(aold)) { asum -= aold; count -= 1; }                                \
-        out[i] = (T)(count >= min_count ? asum : NAN);                                 \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_var (STD=0) / move_std (STD=1), numbagg/moving.py:123-181 */
-#define DEF_MOVE_VAR(T, SFX, NAME, STD)                                               \
-  EXPORT int orc_move_##NAME##_##SFX(const T* a_, T* out_, int64_t rows, int64_t n,    \
-                                     int64_t window, int64_t min_count, int nthreads) { \
-    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
-    for (int64_t r = 0; r < rows; ++r) {                                               \
-      const T* a = a_ + r * n; T* out = out_ + r * n;                                  \
-      double asum = 0.0, asum_sq = 0.0; int64_t count = 0;                             \
-      int64_t mc = min_count > 2 ? min_count : 2;                                      \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double ai = (double)a[i];                                                      \
-        if (i >= window) {                                                             \
-          double aold = (double)a[i - window];                                         \
-          if (!isnan(aold)) { asum -= aold; asum_sq -= aold * aold; count -= 1; }      \
-        }                                                                              \
-        if (!isnan(ai)) { asum += ai; asum_sq += ai * ai; count += 1; }                \
-        if (count >= mc) {                                                             \
-          double variance = (asum_sq - (asum * asum) / (double)count) /                \
-                            (double)(count - 1);                                       \
-          out[i] = (T)(STD ? sqrt(variance) : variance);                               \
-        } else {                                                                       \
-          out[i] = (T)NAN;                                                             \
-        }                                                                              \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_cov, numbagg/moving.py:184-220 */
-#define DEF_MOVE_COV(T, SFX)                                                          \
-  EXPORT int orc_move_cov_##SFX(const T* a_, const T* b_, T* out_, int64_t rows,       \
-                                int64_t n, int64_t window, int64_t min_count,          \
-                                int nthreads) {                                        \
-    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
-    for (int64_t r = 0; r < rows; ++r) {                                               \
-      const T* a = a_ + r * n; const T* b = b_ + r * n; T* out = out_ + r * n;         \
-      double asum = 0.0, bsum = 0.0, prodsum = 0.0; int64_t count = 0;                 \
-      int64_t mc = min_count > 2 ? min_count : 2;                                      \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double ai = (double)a[i], bi = (double)b[i];                                   \
-        if (i >= window) {                                                             \
-          double aold = (double)a[i - window], bold = (double)b[i - window];           \
-          if (!(isnan(aold) || isnan(bold))) {                                         \
-            asum -= aold; bsum -= bold; prodsum -= aold * bold; count -= 1;            \
-          }                                                                            \
-        }                                                                              \
-        if (!(isnan(ai) || isnan(bi))) {                                               \
-          asum += ai; bsum += bi; prodsum += ai * bi; count += 1;                      \
-        }                                                                              \
-        if (count >= mc)                                                               \
-          out[i] = (T)((prodsum - asum * bsum / (double)count) / (double)(count - 1)); \
-        else                                                                           \
-          out[i] = (T)NAN;                                                             \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_corr, numbagg/moving.py:223-275 */
-#define DEF_MOVE_CORR(T, SFX)                                                         \
-  EXPORT int orc_move_corr_##SFX(const T* a_, const T* b_, T* out_, int64_t rows,      \
-                                 int64_t n, int64_t window, int64_t min_count,         \
-                                 int nthreads) {                                       \
-    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
-    for (int64_t r = 0; r < rows; ++r) {                                               \
-      const T* a = a_ + r * n; const T* b = b_ + r * n; T* out = out_ + r * n;         \
-      double asum = 0.0, bsum = 0.0, prodsum = 0.0, asum_sq = 0.0, bsum_sq = 0.0;      \
-      int64_t count = 0;                                                               \
-      int64_t mc = min_count > 1 ? min_count : 1;                                      \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double ai = (double)a[i], bi = (double)b[i];                                   \
-        if (i >= window) {                                                             \
-          double aold = (double)a[i - window], bold = (double)b[i - window];           \
-          if (!(isnan(aold) || isnan(bold))) {                                         \
-            asum -= aold; bsum -= bold; prodsum -= aold * bold;                        \
-            asum_sq -= aold * aold; bsum_sq -= bold * bold; count -= 1;                \
-          }                                                                            \
-        }                                                                              \
-        if (!(isnan(ai) || isnan(bi))) {                                               \
-          asum += ai; bsum += bi; prodsum += ai * bi;                                  \
-          asum_sq += ai * ai; bsum_sq += bi * bi; count += 1;                          \
-        }                                                                              \
-        if (count >= mc) {                                                             \
-          double rc = 1.0 / (double)count;                                             \
-          double avg_a = asum * rc, avg_b = bsum * rc;                                 \
-          double var_a = asum_sq * rc - avg_a * avg_a;                                 \
-          double var_b = bsum_sq * rc - avg_b * avg_b;                                 \
-          double cov_ab = prodsum * rc - avg_a * avg_b;                                \
-          double vv = var_a * var_b;                                                   \
-          out[i] = (T)(vv > 0 ? cov_ab / sqrt(vv) : NAN);                              \
-        } else {                                                                       \
-          out[i] = (T)NAN;                                                             \
-        }                                                                              \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-DEF_MOVE_MEAN(double, f64)
-DEF_MOVE_MEAN(float, f32)
-DEF_MOVE_SUM(double, f64)
-DEF_MOVE_SUM(float, f32)
-DEF_MOVE_VAR(double, f64, var, 0)
-DEF_MOVE_VAR(float, f32, var, 0)
-DEF_MOVE_VAR(double, f64, std, 1)
-DEF_MOVE_VAR(float, f32, std, 1)
-DEF_MOVE_COV(double, f64)
-DEF_MOVE_COV(float, f32)
-DEF_MOVE_CORR(double, f64)
-DEF_MOVE_CORR(float, f32)
-
-/* ------------------------------------------------------------------------------ */
-/* Exponentially weighted: numbagg/moving_exp.py                                   */
-/* alpha is read as alpha[r * alpha_row_stride + i]; a stride of 0 shares one       */
-/* 1-D alpha across rows (the scalar / 1-D alpha forms, numbagg/decorators.py:398). */
-/* ------------------------------------------------------------------------------ */
-
-#define EXP_PROLOGUE(T)                                                                \
-  _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")      \
-  for (int64_t r = 0; r < rows; ++r) {                                                 \
-    const T* a = a_ + r * n; T* out = out_ + r * n;                                    \
-    const T* alpha = alpha_ + r * alpha_row_stride;                                    \
-    double min_weight = (double)min_weight_;
-
-/* move_exp_nancount, numbagg/moving_exp.py:12-38 */
-#define DEF_EXP_COUNT(T, SFX)                                                         \
-  EXPORT int orc_move_exp_nancount_##SFX(const T* a_, const T* alpha_,                 \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP_PROLOGUE(T)                                                                    \
-      double count = 0.0, weight = 0.0;                                                \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double a_i = (double)a[i]; double alpha_i = (double)alpha[i];                  \
-        double decay = 1.0 - alpha_i;                                                  \
-        count *= decay; weight *= decay;                                               \
-        if (!isnan(a_i)) { count += 1; weight += alpha_i; }                            \
-        out[i] = (T)(weight >= min_weight ? count : NAN);                              \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_exp_nanmean, numbagg/moving_exp.py:41-71 */
-#define DEF_EXP_MEAN(T, SFX)                                                          \
-  EXPORT int orc_move_exp_nanmean_##SFX(const T* a_, const T* alpha_,                  \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP_PROLOGUE(T)                                                                    \
-      double numer = 0.0, denom = 0.0, weight = 0.0;                                   \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double a_i = (double)a[i]; double alpha_i = (double)alpha[i];                  \
-        double decay = 1.0 - alpha_i;                                                  \
-        numer *= decay; denom *= decay; weight *= decay;                               \
-        if (!isnan(a_i)) { numer += a_i; denom += 1.0; weight += alpha_i; }            \
-        out[i] = (T)(weight >= min_weight ? numer / denom : NAN);                      \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_exp_nansum, numbagg/moving_exp.py:74-102 */
-#define DEF_EXP_SUM(T, SFX)                                                           \
-  EXPORT int orc_move_exp_nansum_##SFX(const T* a_, const T* alpha_,                   \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP_PROLOGUE(T)                                                                    \
-      double numer = 0.0, weight = 0.0; int zero_count = 1;                            \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double a_i = (double)a[i]; double alpha_i = (double)alpha[i];                  \
-        double decay = 1.0 - alpha_i;                                                  \
-        numer *= decay; weight *= decay;                                               \
-        if (!isnan(a_i)) { zero_count = 0; numer += a_i; weight += alpha_i; }          \
-        out[i] = (T)((weight >= min_weight && !zero_count) ? numer : NAN);             \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_exp_nanvar (STD=0) / move_exp_nanstd (STD=1), numbagg/moving_exp.py:105-223 */
-#define DEF_EXP_VAR(T, SFX, NAME, STD)                                                \
-  EXPORT int orc_move_exp_##NAME##_##SFX(const T* a_, const T* alpha_,                 \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP_PROLOGUE(T)                                                                    \
-      double sum_x_2 = 0.0, sum_x = 0.0, sum_weight = 0.0, sum_weight_2 = 0.0;         \
-      double weight = 0.0;                                                             \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double a_i = (double)a[i]; double alpha_i = (double)alpha[i];                  \
-        double decay = 1.0 - alpha_i;                                                  \
-        sum_x_2 *= decay; sum_x *= decay; sum_weight *= decay;                         \
-        sum_weight_2 *= decay * decay; weight *= decay;                                \
-        if (!isnan(a_i)) {                                                             \
-          sum_x_2 += a_i * a_i; sum_x += a_i; sum_weight += 1.0;                       \
-          sum_weight_2 += 1.0; weight += alpha_i;                                      \
-        }                                                                              \
-        double m = sum_x / sum_weight;                                                 \
-        double var_biased = (sum_x_2 / sum_weight) - m * m;                            \
-        double bias = 1.0 - sum_weight_2 / (sum_weight * sum_weight);                  \
-        if (weight >= min_weight && bias > 0) {                                        \
-          double v = var_biased / bias;                                                \
-          out[i] = (T)(STD ? sqrt(v) : v);                                             \
-        } else {                                                                       \
-          out[i] = (T)NAN;                                                             \
-        }                                                                              \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-#define EXP2_PROLOGUE(T)                                                               \
-  _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")      \
-  for (int64_t r = 0; r < rows; ++r) {                                                 \
-    const T* a1 = a1_ + r * n; const T* a2 = a2_ + r * n; T* out = out_ + r * n;       \
-    const T* alpha = alpha_ + r * alpha_row_stride;                                    \
-    double min_weight = (double)min_weight_;
-
-/* move_exp_nancov, numbagg/moving_exp.py:226-272 */
-#define DEF_EXP_COV(T, SFX)                                                           \
-  EXPORT int orc_move_exp_nancov_##SFX(const T* a1_, const T* a2_, const T* alpha_,    \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP2_PROLOGUE(T)                                                                   \
-      double sum_x1 = 0.0, sum_x2 = 0.0, sum_x1x2 = 0.0, sum_weight = 0.0;             \
-      double sum_weight_2 = 0.0, weight = 0.0;                                         \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double x1 = (double)a1[i], x2 = (double)a2[i];                                 \
-        double alpha_i = (double)alpha[i]; double decay = 1.0 - alpha_i;               \
-        sum_x1 *= decay; sum_x2 *= decay; sum_x1x2 *= decay; sum_weight *= decay;      \
-        sum_weight_2 *= decay * decay; weight *= decay;                                \
-        if (!(isnan(x1) || isnan(x2))) {                                               \
-          sum_x1 += x1; sum_x2 += x2; sum_x1x2 += x1 * x2;                             \
-          sum_weight += 1; sum_weight_2 += 1; weight += alpha_i;                       \
-        }                                                                              \
-        double cov_biased = (sum_x1x2 - (sum_x1 * sum_x2 / sum_weight)) / sum_weight;  \
-        double bias = 1.0 - sum_weight_2 / (sum_weight * sum_weight);                  \
-        out[i] = (T)((weight >= min_weight && bias > 0) ? cov_biased / bias : NAN);    \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-/* move_exp_nancorr, numbagg/moving_exp.py:275-335 */
-#define DEF_EXP_CORR(T, SFX)                                                          \
-  EXPORT int orc_move_exp_nancorr_##SFX(const T* a1_, const T* a2_, const T* alpha_,   \
-      int64_t alpha_row_stride, T min_weight_, T* out_, int64_t rows, int64_t n,       \
-      int nthreads) {                                                                  \
-    EXP2_PROLOGUE(T)                                                                   \
-      double sum_x1 = 0.0, sum_x2 = 0.0, sum_x1x2 = 0.0, sum_weight = 0.0;             \
-      double sum_weight_2 = 0.0, weight = 0.0, sum_x1_2 = 0.0, sum_x2_2 = 0.0;         \
-      for (int64_t i = 0; i < n; ++i) {                                                \
-        double x1 = (double)a1[i], x2 = (double)a2[i];                                 \
-        double alpha_i = (double)alpha[i]; double decay = 1.0 - alpha_i;               \
-        sum_x1 *= decay; sum_x2 *= decay; sum_x1x2 *= decay; sum_weight *= decay;      \
-        sum_weight_2 *= decay * decay; weight *= decay;                                \
-        sum_x1_2 *= decay; sum_x2_2 *= decay;                                          \
-        if (!(isnan(x1) || isnan(x2))) {                                               \
-          sum_x1 += x1; sum_x2 += x2; sum_x1x2 += x1 * x2;                             \
-          sum_weight += 1; sum_weight_2 += 1; weight += alpha_i;                       \
-          sum_x1_2 += x1 * x1; sum_x2_2 += x2 * x2;                                    \
-        }                                                                              \
-        double cov = sum_x1x2 - (sum_x1 * sum_x2 / sum_weight);                        \
-        double var_a1 = sum_x1_2 - (sum_x1 * sum_x1 / sum_weight);                     \
-        double var_a2 = sum_x2_2 - (sum_x2 * sum_x2 / sum_weight);                     \
-        double bias = 1.0 - sum_weight_2 / (sum_weight * sum_weight);                  \
-        if (weight >= min_weight && bias > 0) {                                        \
-          double den = sqrt(var_a1 * var_a2);                                          \
-          out[i] = (T)(den > 0 ? cov / den : NAN);                                     \
-        } else {                                                                       \
-          out[i] = (T)NAN;                                                             \
-        }                                                                              \
-      }                                                                                \
-    }                                                                                  \
-    return 0;                                                                          \
-  }
-
-DEF_EXP_COUNT(double, f64)
-DEF_EXP_COUNT(float, f32)
-DEF_EXP_MEAN(double, f64)
-DEF_EXP_MEAN(float, f32)
-DEF_EXP_SUM(double, f64)
-DEF_EXP_SUM(float, f32)
-DEF_EXP_VAR(double, f64, nanvar, 0)
-DEF_EXP_VAR(float, f32, nanvar, 0)
-DEF_EXP_VAR(double, f64, nanstd, 1)
-DEF_EXP_VAR(float, f32, nanstd, 1)
-DEF_EXP_COV(double, f64)
-DEF_EXP_COV(float, f32)
-DEF_EXP_CORR(double, f64)
-DEF_EXP_CORR(float, f32)
+#define CAT2(a, b) a##b
+#define ACC double
+#define ACC_SQRT sqrt
+#define ONAME(f, s) CAT2(orc_##f##_, s)
+#include "scan_loops.inc"
+#undef ACC
+#undef ACC_SQRT
+#undef ONAME
+#define ACC long double
+#define ACC_SQRT sqrtl
+#define ONAME(f, s) CAT2(orc_##f##_ext_, s)
+#include "scan_loops.inc"
+#undef ACC
+#undef ACC_SQRT
+#undef ONAME
 
 /* ------------------------------------------------------------------------------ */
 /* Fills: numbagg/funcs.py:294-326.  The carried `current` is float64 in numba     */
@@ -840,3 +517,5 @@ DEF_GROUP_ALL_INT(int64_t, i64, INT_NAN_i64)
 
 DEF_MOVE_MATRIX(double, f64)
 DEF_MOVE_MATRIX(float, f32)
+/* extended precision (long double arrays and accumulators) */
+DEF_MOVE_MATRIX(long double, ld)

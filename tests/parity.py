@@ -55,6 +55,50 @@ def assert_scaled_close(got, ref, scale, tol, allow=None, what=""):
     return r
 
 
+def parity_error(got, ref, ext, scale, allow=None):
+    """Deviation of `got` from the reference `ref` beyond the reference's own rounding
+    error, measured against the extended-precision result `ext`:
+        excess = max(0, |got - ref| - |ref - ext|) / max(|ref|, S)
+    and the accuracy of `got` itself, |got - ext| / max(|ext|, S)."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    ext = np.asarray(ext, dtype=np.float64)
+    scale = np.broadcast_to(np.asarray(scale, dtype=np.float64), ref.shape)
+    gn, rn = np.isnan(got), np.isnan(ref)
+    allow = np.zeros(ref.shape, bool) if allow is None else np.asarray(allow, bool)
+    nan_bad = (gn != rn) & ~allow
+    both = ~gn & ~rn & ~allow
+    inf = both & (np.isinf(ref) | np.isinf(got))
+    inf_bad = inf & (got != ref)
+    fin = both & ~inf & ~np.isnan(ext) & ~np.isinf(ext)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        denom = np.fmax(np.abs(ref[fin]), np.abs(scale[fin]))
+        excess = np.maximum(0.0, np.abs(got[fin] - ref[fin]) - np.abs(ref[fin] - ext[fin]))
+        err = np.where(denom > 0, excess / np.where(denom > 0, denom, 1), excess)
+        dext = np.fmax(np.abs(ext[fin]), np.abs(scale[fin]))
+        acc = np.abs(got[fin] - ext[fin])
+        acc = np.where(dext > 0, acc / np.where(dext > 0, dext, 1), acc)
+        refacc = np.abs(ref[fin] - ext[fin])
+        refacc = np.where(dext > 0, refacc / np.where(dext > 0, dext, 1), refacc)
+    return {
+        "nan_mismatch": int(nan_bad.sum()),
+        "inf_mismatch": int(inf_bad.sum()),
+        "max_excess": float(err.max()) if err.size else 0.0,
+        "gpu_vs_ext": float(acc.max()) if acc.size else 0.0,
+        "ref_vs_ext": float(refacc.max()) if refacc.size else 0.0,
+        "allowed": int(allow.sum()),
+        "n": int(ref.size),
+    }
+
+
+def assert_parity(got, ref, ext, scale, tol, allow=None, what=""):
+    r = parity_error(got, ref, ext, scale, allow)
+    assert r["nan_mismatch"] == 0, f"{what}: NaN placement differs at {r['nan_mismatch']} positions ({r})"
+    assert r["inf_mismatch"] == 0, f"{what}: inf differs ({r})"
+    assert r["max_excess"] <= tol, f"{what}: deviation beyond the reference's own error {r['max_excess']:.3g} > {tol:g} ({r})"
+    return r
+
+
 def assert_bit_equal(got, ref, what=""):
     got = np.asarray(got)
     ref = np.asarray(ref)
@@ -80,12 +124,17 @@ def _cond(msq, var):
 
 
 def move_scale(name, a, b, window, axis=-1):
+    """Scales over a span of 2*window: the reference's running sums still carry the
+    rounding residue of values that have just left the window."""
     absa = np.abs(np.asarray(a, dtype=np.float64))
+    n = absa.shape[axis]
+    w2 = min(2 * window, n)
+    cnt = oracle.move("move_sum", (~np.isnan(absa)).astype(np.float64), window=window, min_count=0, axis=axis)
     if name == "move_sum":
-        return oracle.move("move_sum", absa, window=window, min_count=0, axis=axis)
+        return oracle.move("move_sum", absa, window=w2, min_count=0, axis=axis)
     if name == "move_mean":
-        return oracle.move("move_mean", absa, window=window, min_count=1, axis=axis)
-    sq = oracle.move("move_mean", absa * absa, window=window, min_count=1, axis=axis)
+        return oracle.move("move_sum", absa, window=w2, min_count=0, axis=axis) / np.maximum(cnt, 1)
+    sq = oracle.move("move_sum", absa * absa, window=w2, min_count=0, axis=axis) / np.maximum(cnt - 1, 1)
     if name == "move_var":
         return sq
     if name == "move_std":
@@ -93,7 +142,7 @@ def move_scale(name, a, b, window, axis=-1):
         with np.errstate(invalid="ignore", divide="ignore"):
             return np.fmax(np.sqrt(sq), sq / std)
     absb = np.abs(np.asarray(b, dtype=np.float64))
-    sqb = oracle.move("move_mean", absb * absb, window=window, min_count=1, axis=axis)
+    sqb = oracle.move("move_sum", absb * absb, window=w2, min_count=0, axis=axis) / np.maximum(cnt - 1, 1)
     if name == "move_cov":
         return np.sqrt(sq * sqb)
     # move_corr

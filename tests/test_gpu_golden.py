@@ -9,10 +9,12 @@ import numpy as np
 import pytest
 
 import numbagg_gb300 as nb
+import oracle
 from tests.parity import (
     F32_TOL,
     F64_TOL,
     assert_bit_equal,
+    assert_parity,
     assert_scaled_close,
     exp_degenerate,
     exp_scale,
@@ -43,7 +45,8 @@ def test_move_golden(golden, fname):
         assert got.dtype == want.dtype
         scale = move_scale(fname, x, b, w)
         allow = move_degenerate(fname, x, b, w)
-        assert_scaled_close(got, want, scale, TOL[dt], allow, key)
+        ext = oracle.move(fname, x, b, window=w, min_count=mc, ext=True)
+        assert_parity(got, want, ext, scale, TOL[dt], allow, key)
 
 
 @pytest.mark.parametrize(
@@ -70,7 +73,8 @@ def test_move_exp_golden(golden, fname):
         want = golden[key]
         scale = exp_scale(fname, x, b, alpha)
         allow = exp_degenerate(fname, x, b, alpha, mw)
-        assert_scaled_close(got, want, scale, TOL[dt], allow, key)
+        ext = oracle.move_exp(fname, x, b, alpha=alpha, min_weight=mw, ext=True)
+        assert_parity(got, want, ext, scale, TOL[dt], allow, key)
 
 
 @pytest.mark.parametrize("fname", ["ffill", "bfill"])
@@ -141,11 +145,21 @@ def test_move_matrix_golden(golden, fname):
         got = func(a, window=int(w), min_count=None if mc == "None" else int(mc))
         want = golden[key]
         assert got.shape == want.shape and got.dtype == want.dtype
+        mcv = None if mc == "None" else int(mc)
+        ext = oracle.move_matrix(fname, a.astype(np.float64), window=int(w), min_count=mcv, ext=True)
         if dt == "f64":
             scale = np.ones_like(want) if fname == "move_corrmatrix" else np.nanmax(np.abs(want)) * np.ones_like(want)
-            assert_scaled_close(got, want, scale, F64_TOL, None, key)
+            assert_parity(got, want, ext, scale, F64_TOL, None, key)
         else:
             # the reference accumulates float32 in float32; this implementation in
             # float64, so the float32 reference carries the larger error
             scale = np.ones_like(want) if fname == "move_corrmatrix" else np.nanmax(np.abs(want)) * np.ones_like(want)
-            assert_scaled_close(got, want, scale, 2e-4, None, key)
+            # a window holding <= 2 complete pairs has correlation +-1 exactly; the
+            # float32-accumulated reference returns its rounding noise there
+            v = (~np.isnan(a)).astype(np.int64)
+            pairs = np.einsum("ti,tj->tij", v, v)
+            csum = np.cumsum(pairs, axis=0)
+            win = csum.copy()
+            win[int(w):] -= csum[: -int(w)]
+            allow = (win <= 2) if fname == "move_corrmatrix" else None
+            assert_parity(got, want, ext, scale, 2e-4, allow, key)

@@ -12,6 +12,7 @@ from tests.parity import (
     F32_TOL,
     F64_TOL,
     assert_bit_equal,
+    assert_parity,
     assert_scaled_close,
     exp_degenerate,
     exp_scale,
@@ -49,8 +50,12 @@ def test_move_vs_oracle(fname, dtype, window, min_count):
     func = getattr(nb, fname)
     got = func(x, y, window=window, min_count=min_count) if y is not None else func(x, window=window, min_count=min_count)
     want = oracle.move(fname, x, y, window=window, min_count=min_count)
+    ext = oracle.move(fname, x, y, window=window, min_count=min_count, ext=True)
     tol = F64_TOL if dtype == np.float64 else F32_TOL
-    assert_scaled_close(got, want, move_scale(fname, x, y, window), tol, move_degenerate(fname, x, y, window), fname)
+    r = assert_parity(got, want, ext, move_scale(fname, x, y, window), tol, move_degenerate(fname, x, y, window), fname)
+    # the exact sums make the GPU at least as close to the extended result as the reference
+    if dtype == np.float64:
+        assert r["gpu_vs_ext"] <= max(r["ref_vs_ext"], 1e-14), r
 
 
 @pytest.mark.parametrize("fname", ["move_mean", "move_std", "move_corr"])
@@ -62,14 +67,16 @@ def test_move_axis_and_torch(fname):
     for axis in (0, 1, -1):
         got = func(x, y, window=3, axis=axis) if two else func(x, window=3, axis=axis)
         want = oracle.move(fname, x, y if two else None, window=3, axis=axis)
-        assert_scaled_close(got, want, move_scale(fname, x, y, 3, axis), F64_TOL, move_degenerate(fname, x, y, 3, axis), f"{fname} axis={axis}")
+        ext = oracle.move(fname, x, y if two else None, window=3, axis=axis, ext=True)
+        assert_parity(got, want, ext, move_scale(fname, x, y, 3, axis), F64_TOL, move_degenerate(fname, x, y, 3, axis), f"{fname} axis={axis}")
     # torch CUDA tensors in, torch CUDA tensors out
     xt = torch.from_numpy(x).cuda()
     yt = torch.from_numpy(y).cuda()
     res = func(xt, yt, window=3, axis=0) if two else func(xt, window=3, axis=0)
     assert isinstance(res, torch.Tensor) and res.is_cuda
     want = oracle.move(fname, x, y if two else None, window=3, axis=0)
-    assert_scaled_close(res.cpu().numpy(), want, move_scale(fname, x, y, 3, 0), F64_TOL, move_degenerate(fname, x, y, 3, 0), fname)
+    ext = oracle.move(fname, x, y if two else None, window=3, axis=0, ext=True)
+    assert_parity(res.cpu().numpy(), want, ext, move_scale(fname, x, y, 3, 0), F64_TOL, move_degenerate(fname, x, y, 3, 0), fname)
 
 
 def test_move_edge_cases():
@@ -81,7 +88,8 @@ def test_move_edge_cases():
     for fname in ("move_sum", "move_mean", "move_var", "move_std"):
         got = getattr(nb, fname)(x, window=17, min_count=0)
         want = oracle.move(fname, x, window=17, min_count=0)
-        assert_scaled_close(got, want, move_scale(fname, x, None, 17), F64_TOL, None, fname)
+        ext = oracle.move(fname, x, window=17, min_count=0, ext=True)
+        assert_parity(got, want, ext, move_scale(fname, x, None, 17), F64_TOL, None, fname)
     ints = np.arange(50, dtype=np.int64).reshape(5, 10)
     got = nb.move_sum(ints, window=3)
     assert got.dtype == np.float64
@@ -110,9 +118,10 @@ def test_move_exp_vs_oracle(fname, dtype, alpha, min_weight):
     func = getattr(nb, fname)
     got = func(x, y, alpha=alpha, min_weight=min_weight) if y is not None else func(x, alpha=alpha, min_weight=min_weight)
     want = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight)
+    ext = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight, ext=True)
     tol = F64_TOL if dtype == np.float64 else F32_TOL
     allow = exp_degenerate(fname, x, y, alpha, min_weight)
-    r = assert_scaled_close(got, want, exp_scale(fname, x, y, alpha), tol, allow, fname)
+    r = assert_parity(got, want, ext, exp_scale(fname, x, y, alpha), tol, allow, fname)
     assert r["allowed"] <= 0.001 * r["n"] + 20
 
 
@@ -126,7 +135,8 @@ def test_move_exp_alpha_forms(fname):
     alphas = np.linspace(0.01, 0.6, 3000)
     got1 = func(x, y, alpha=alphas) if two else func(x, alpha=alphas)
     want1 = oracle.move_exp(fname, x, y if two else None, alpha=alphas)
-    assert_scaled_close(got1, want1, exp_scale(fname, x, y, alphas), F64_TOL, exp_degenerate(fname, x, y, alphas, 0.0), fname)
+    ext1 = oracle.move_exp(fname, x, y if two else None, alpha=alphas, ext=True)
+    assert_parity(got1, want1, ext1, exp_scale(fname, x, y, alphas), F64_TOL, exp_degenerate(fname, x, y, alphas, 0.0), fname)
     full = np.broadcast_to(alphas, x.shape).copy()
     got2 = func(x, y, alpha=full) if two else func(x, alpha=full)
     assert_bit_equal(got2, got1, "N-D alpha vs 1-D alpha")
@@ -322,12 +332,13 @@ def test_move_matrix_vs_oracle(fname, dtype):
     for window, mc in [(50, 40), (7, None), (700, 1)]:
         got = getattr(nb, fname)(a, window=window, min_count=mc)
         want = oracle.move_matrix(fname, a.astype(np.float64), window=window, min_count=mc)
+        ext = oracle.move_matrix(fname, a.astype(np.float64), window=window, min_count=mc, ext=True)
         tol = F64_TOL if dtype == np.float64 else F32_TOL
         if fname == "move_covmatrix":
             scale = np.sqrt(np.abs(np.einsum("...ii->...i", np.nan_to_num(want)))[..., :, None] * np.abs(np.einsum("...ii->...i", np.nan_to_num(want)))[..., None, :]) + 1e-300
         else:
             scale = np.ones_like(want)
-        assert_scaled_close(got, want.astype(dtype), scale, tol, None, f"{fname} w={window}")
+        assert_parity(got, want.astype(dtype), ext, scale, tol, None, f"{fname} w={window}")
 
 
 def test_move_matrix_known_answers():
