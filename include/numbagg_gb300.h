@@ -39,6 +39,7 @@ extern "C" {
 #define NBG_WORKSPACE_TOO_SMALL 3
 #define NBG_LOOKBACK_TIMEOUT 4 /* recorded on the device; read with nbg_workspace_error */
 #define NBG_UNSUPPORTED 5
+#define NBG_TOO_LARGE 6 /* beyond the fixed scratch of an allocation-free entry point */
 
 NBG_API int nbg_version(void);
 NBG_API const char* nbg_status_string(int status);
@@ -126,6 +127,24 @@ NBG_DECL_FILL(double, f64)
 NBG_DECL_FILL(float, f32)
 NBG_DECL_FILL(int, i32)
 NBG_DECL_FILL(long long, i64)
+
+/* Allocation-free forward fill (float64).  No counterpart in numbagg: it exists for
+ * callers that may not allocate device memory -- a host application that owns all GPU
+ * memory and lends this library only the input and output buffers (a database or
+ * stream engine running it as a user-defined function under a fixed budget), or a
+ * latency-critical path that must never reach cudaMalloc/cudaFree, which can
+ * synchronise the device.  Same results as nbg_ffill_f64; no workspace argument and
+ * no allocation of any kind.  The look-back state lives in a 4 MiB array inside the
+ * library's device image (every GPU that loads the library keeps it until the
+ * process exits), so a call may cover at most that many tiles: rows x ceil(n / 4096)
+ * tiles within nbg_ffill_noalloc_max_scratch_bytes(); larger problems return
+ * NBG_TOO_LARGE without launching.  The first call on a device looks up and clears
+ * the array on `stream`; make that first call before any stream capture.  All calls
+ * on a device share the one array: calls that overlap on the GPU (different streams,
+ * or concurrent threads) race and must be serialised by the caller. */
+NBG_API size_t nbg_ffill_noalloc_max_scratch_bytes(void);
+NBG_API int nbg_ffill_f64_noalloc(const double* a, double* out, long long rows, long long n,
+                                  long long limit, void* stream);
 
 /* ---- grouped reductions ----------------------------------------------------------------
  * Replaces the gufuncs built by groupndreduce (numbagg/decorators.py:490-674) from

@@ -25,6 +25,7 @@ STATUS = {
     3: "workspace missing or too small",
     4: "look-back wait exceeded its bound",
     5: "unsupported shape or dtype",
+    6: "problem larger than the fixed scratch of the allocation-free entry point",
 }
 
 _lib: ctypes.CDLL | None = None
@@ -56,6 +57,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     sig("nbg_move_workspace_bytes", c_sz, c_ll, c_ll)
     sig("nbg_move_exp_workspace_bytes", c_sz, c_ll, c_ll)
     sig("nbg_fill_workspace_bytes", c_sz, c_ll, c_ll)
+    sig("nbg_ffill_noalloc_max_scratch_bytes", c_sz)
+    sig("nbg_ffill_f64_noalloc", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp)
     sig("nbg_group_workspace_bytes", c_sz, c_i, c_ll, c_ll, c_ll)
     for dt in ("f64", "f32"):
         for f in ("move_sum", "move_mean", "move_var", "move_std"):

@@ -24,6 +24,7 @@ const char* nbg_status_string(int status) {
     case kWorkspaceTooSmall: return "workspace missing or too small";
     case kLookbackTimeout: return "look-back wait exceeded its bound";
     case kUnsupported: return "unsupported shape or dtype";
+    case kTooLarge: return "problem larger than the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }

@@ -16,6 +16,8 @@
 // NaN, that makes the fill an element-wise copy through double.
 #include "nbg_common.cuh"
 
+#include <mutex>
+
 namespace nbg {
 namespace fill {
 
@@ -255,5 +257,66 @@ NBG_FILL_F(double, f64)
 NBG_FILL_F(float, f32)
 NBG_FILL_I(int, i32)
 NBG_FILL_I(long long, i64)
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Allocation-free forward fill
+//
+// Some callers cannot allocate device memory at all: a host application that owns
+// every byte of GPU memory and hands this library only its input and output buffers
+// (a database or stream engine running it as a user-defined function under a fixed
+// memory budget), or a latency-critical path that must never reach cudaMalloc /
+// cudaFree, which can synchronise the whole device.  For them nbg_ffill_f64_noalloc
+// keeps the look-back state in a fixed array in device memory that is part of this
+// library's image (every GPU that loads the library holds it until the process exits)
+// instead of a caller-provided workspace.
+// ---------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = static_cast<size_t>(4) << 20;  // 4 MiB per device
+__device__ __align__(256) unsigned char g_fill_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The first call on a
+// device looks the address up and zero-fills the array on `stream` (the fill kernel
+// that follows on the same stream sees it cleared).  In host code the array's name
+// is only a host-side stand-in, never a device address.
+int noalloc_scratch(cudaStream_t stream, void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return kLaunchError;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_fill_noalloc_scratch) != cudaSuccess || !p) return kLaunchError;
+    if (cudaMemsetAsync(p, 0, kNoAllocScratchBytes, stream) != cudaSuccess) return kLaunchError;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t nbg_ffill_noalloc_max_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+int nbg_ffill_f64_noalloc(const double* a, double* out, long long rows, long long n, long long limit,
+                          void* stream) {
+  if (rows < 0 || n < 0 || limit < 0) return kInvalidArgument;
+  if (rows == 0 || n == 0) return kOk;
+  if (!a || !out) return kInvalidArgument;
+  const long long tpr = fill_tiles_per_row(n);
+  if (workspace_bytes(rows * tpr) > kNoAllocScratchBytes) return kTooLarge;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  const int st = noalloc_scratch(s, &scratch);
+  if (st != kOk) return st;
+  return launch_fill<double, false>(a, out, rows, n, limit, scratch, kNoAllocScratchBytes, s);
+}
 
 }  // extern "C"

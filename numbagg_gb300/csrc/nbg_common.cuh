@@ -42,6 +42,7 @@ enum Status : int {
   kWorkspaceTooSmall = 3,
   kLookbackTimeout = 4,
   kUnsupported = 5,
+  kTooLarge = 6,
 };
 
 // ---------------------------------------------------------------------------------
