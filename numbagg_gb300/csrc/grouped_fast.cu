@@ -1,0 +1,931 @@
+// Labelled reductions, fast paths (numbagg/grouped.py:7-244).
+//
+// values (rows, m), labels (m,) shared by every row, out (rows, K).  Three strategies,
+// chosen from K:
+//
+//  * tiny K (<= 16): every thread owns a private copy of the K bins in shared memory
+//    (no atomics).  A warp works through tiles of 32 x 16 columns; within a tile every
+//    value is turned into a 64-bit fixed-point integer at the scale of the tile's
+//    largest exponent (53 significant bits, exact sums of up to 1024 terms), then the
+//    lanes' bins are summed with warp shuffles and added, as float64, to a per-warp
+//    accumulator held by lane k for bin k.
+//  * medium K (bins fit in shared memory): the bins of a CTA are shared and updated
+//    with 64-bit shared-memory atomics on fixed-point integers at a CTA scale that
+//    grows with the largest exponent seen; at the end of the chunk (or every 2^15
+//    columns when the chunk's label histogram shows a label that frequent) the bins
+//    are flushed, as float64, into the CTA's own partial in global memory.
+//  * large K (e.g. 10^6): float64 reductions straight into per-row accumulators in
+//    global memory.  CTAs are ordered row by row, so only the rows in flight (a few
+//    tens of MB of accumulators) are live and they stay in L2.
+//
+// Counts come from the labels where possible: the number of columns with label k is
+// the same for every row, so the valid count is that label histogram (computed once
+// per call) minus the NaN count, and only NaN elements pay for a counting atomic.
+//
+// Selection (argmax / argmin / max / min) keeps the reference's strict comparison on
+// float64 values, the first index winning ties (numbagg/grouped.py:62, :86, :221,
+// :239): an element is the pair (order key of its float64 value with -0.0 == +0.0,
+// column index) and a bin keeps the best pair -- larger key, then smaller index.
+// Private bins are updated in column order; shared and global bins with a 128-bit
+// compare-and-swap issued only when the element improves on the current pair.
+// first / last are a minimum / maximum of the column index.  All of these are exact.
+#include "grouped_common.cuh"
+
+namespace nbg {
+namespace grouped {
+
+constexpr int FT = 256;
+constexpr int kTinyK = 16;
+constexpr int kTileCols = 32 * 16;   // columns of one warp tile (tiny path)
+constexpr int kCtaCols = FT * 8;     // columns of one CTA tile (medium / large paths)
+
+struct MomPart {  // one bin of one chunk: float64 sums, valid count, infinities seen
+  double s1, s2;
+  long long cnt;
+  int pinf, ninf;
+};
+struct SelPart {
+  unsigned long long key, idx;
+};
+
+template <int F>
+struct Need {
+  static constexpr bool s1 = F == kSum || F == kMean || F == kVar || F == kStd;
+  static constexpr bool s2 = F == kVar || F == kStd || F == kSumSq;
+  static constexpr bool cnt = F == kCount || F == kMean || F == kVar || F == kStd;
+  static constexpr bool varlike = F == kVar || F == kStd;
+};
+
+NBG_DEVICE int bexp(double x) {
+  const int e = static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(x)) >> 52) & 0x7ff);
+  return e ? e : 1;
+}
+NBG_DEVICE unsigned long long mant(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long m = b & 0x000fffffffffffffull;
+  return ((b >> 52) & 0x7ff) ? (m | 0x0010000000000000ull) : m;
+}
+NBG_DEVICE bool is_inf_d(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffull) == 0x7ff0000000000000ull;
+}
+// |x| >= 2^512: the reference's x**2 overflows
+NBG_DEVICE bool sq_overflows(double x) { return bexp(x) >= 1023 + 512; }
+
+// mantissa aligned to scale exponent E >= e, then shifted right by `drop` more bits
+NBG_DEVICE unsigned long long aligned(double x, int E, int drop) {
+  const int sh = E - bexp(x) + drop;
+  return sh >= 64 ? 0ull : (mant(x) >> sh);
+}
+// (a * a) >> s for a < 2^53
+NBG_DEVICE unsigned long long square_shift(unsigned long long a, int s) {
+  const unsigned long long lo = a * a, hi = __umul64hi(a, a);
+  if (s >= 64) return hi >> (s - 64);
+  return (hi << (64 - s)) | (lo >> s);
+}
+NBG_DEVICE long long signed_of(double x, unsigned long long mag) {
+  return __double_as_longlong(x) < 0 ? -static_cast<long long>(mag) : static_cast<long long>(mag);
+}
+// v * 2^L as a double
+NBG_DEVICE double fix_to_double(long long v, int L) { return scalbn(__ll2double_rn(v), L); }
+
+// Fixed-point formats.  tiny: value = aligned(x, E, 0) * 2^(E - 1075)     (53 bits)
+//                              square = (a*a) >> 53  * 2^(2(E - 1075) + 53)
+//                       medium: value = aligned(x, E, 5) * 2^(E - 1070)     (48 bits)
+//                              square = (a*a) >> 58  * 2^(2(E - 1075) + 58)
+// where a = aligned(x, E, 0).  Headroom: 10 bits (tiny), 15 bits (medium).
+
+template <typename V>
+NBG_DEVICE bool valid_value(V v) { return !is_nan(v); }
+
+template <int F>
+NBG_DEVICE unsigned long long sel_key(double x) {
+  const unsigned long long k = order_key_ieee(x);
+  return (F == kArgMin || F == kMin) ? ~k : k;
+}
+NBG_DEVICE bool better(unsigned long long k1, unsigned long long i1, unsigned long long k2, unsigned long long i2) {
+  return k1 > k2 || (k1 == k2 && i1 < i2);
+}
+
+// 128-bit compare-and-swap of a (key, idx) pair, global or shared (generic address)
+NBG_DEVICE void cas128(unsigned long long* addr, unsigned long long& ck, unsigned long long& ci,
+                       unsigned long long nk, unsigned long long ni, bool shared) {
+  unsigned long long ok, oi;
+  if (shared) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(addr));
+    asm volatile(
+        "{ .reg .b128 c, n, o; mov.b128 c, {%2, %3}; mov.b128 n, {%4, %5};"
+        " atom.shared.cas.b128 o, [%6], c, n; mov.b128 {%0, %1}, o; }"
+        : "=l"(ok), "=l"(oi)
+        : "l"(ck), "l"(ci), "l"(nk), "l"(ni), "r"(a)
+        : "memory");
+  } else {
+    asm volatile(
+        "{ .reg .b128 c, n, o; mov.b128 c, {%2, %3}; mov.b128 n, {%4, %5};"
+        " atom.global.cas.b128 o, [%6], c, n; mov.b128 {%0, %1}, o; }"
+        : "=l"(ok), "=l"(oi)
+        : "l"(ck), "l"(ci), "l"(nk), "l"(ni), "l"(addr)
+        : "memory");
+  }
+  ck = ok;
+  ci = oi;
+}
+
+// keep the better of the pair at addr and (key, idx)
+NBG_DEVICE void sel_update(unsigned long long* addr, unsigned long long key, unsigned long long idx, bool shared) {
+  unsigned long long ck = shared ? *reinterpret_cast<volatile unsigned long long*>(addr) : __ldcg(addr);
+  unsigned long long ci = shared ? *reinterpret_cast<volatile unsigned long long*>(addr + 1) : __ldcg(addr + 1);
+  for (int it = 0; it < 1 << 16 && better(key, idx, ck, ci); ++it) {
+    const unsigned long long ek = ck, ei = ci;
+    cas128(addr, ck, ci, key, idx, shared);
+    if (ck == ek && ci == ei) return;  // swapped in
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// tiny K: lane-private bins
+// ---------------------------------------------------------------------------------
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                      long long m, int K, long long chunk_len, long long chunks,
+                                                      MomPart* __restrict__ parts) {
+  extern __shared__ unsigned char smem_raw[];
+  long long* b1 = reinterpret_cast<long long*>(smem_raw);  // [K][FT]
+  long long* b2 = b1 + K * FT;                              // [K][FT]
+  int* bc = reinterpret_cast<int*>(b2 + K * FT);            // [K][FT]
+  __shared__ double wsum1[FT / 32][kTinyK], wsum2[FT / 32][kTinyK];
+  __shared__ long long wcnt[FT / 32][kTinyK];
+  __shared__ int infs[2][kTinyK];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len;
+  const long long c1 = min(m, c0 + chunk_len);
+  for (int k = 0; k < K; ++k) {
+    b1[k * FT + tid] = 0;
+    b2[k * FT + tid] = 0;
+    bc[k * FT + tid] = 0;
+  }
+  if (tid < 2 * kTinyK) infs[tid / kTinyK][tid % kTinyK] = 0;
+  __syncthreads();
+  const V* vr = values + row * m;
+  double a1 = 0.0, a2 = 0.0;
+  long long ac = 0;
+  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1; base += static_cast<long long>(FT / 32) * kTileCols) {
+    V v[16];
+    int lab[16];
+    int emax = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const long long col = base + j * 32 + lane;
+      const bool in = col < c1;
+      v[j] = in ? vr[col] : V(0);
+      const long long l = in ? static_cast<long long>(labels[col]) : -1;
+      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
+      if (lab[j] >= 0) {
+        const double x = static_cast<double>(v[j]);
+        if (!is_inf_d(x) && !(Need<F>::varlike && sq_overflows(x))) emax = max(emax, bexp(x));
+      }
+    }
+    const int E = max(1, static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax))));
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (lab[j] < 0) continue;
+      const double x = static_cast<double>(v[j]);
+      const int slot = lab[j] * FT + tid;
+      if (Need<F>::cnt) bc[slot] += 1;
+      if (is_inf_d(x) || (Need<F>::varlike && sq_overflows(x))) {
+        atomicAdd(&infs[x > 0 ? 0 : 1][lab[j]], 1);
+        continue;
+      }
+      const unsigned long long a = aligned(x, E, 0);
+      if (Need<F>::s1) b1[slot] += signed_of(x, a);
+      if (Need<F>::s2) b2[slot] += static_cast<long long>(square_shift(a, 53));
+    }
+    __syncwarp();
+    // flush the tile: sum the lanes' bins, lane k adds bin k as float64
+    for (int k = 0; k < K; ++k) {
+      const int slot = k * FT + tid;
+      long long s1 = 0, s2 = 0;
+      int c = 0;
+      if (Need<F>::s1) { s1 = b1[slot]; b1[slot] = 0; }
+      if (Need<F>::s2) { s2 = b2[slot]; b2[slot] = 0; }
+      if (Need<F>::cnt) { c = bc[slot]; bc[slot] = 0; }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        if (Need<F>::s1) s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        if (Need<F>::s2) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        if (Need<F>::cnt) c += __shfl_xor_sync(0xffffffffu, c, o);
+      }
+      if (lane == k) {
+        if (Need<F>::s1 && s1) a1 += fix_to_double(s1, E - 1075);
+        if (Need<F>::s2 && s2) a2 += fix_to_double(s2, 2 * (E - 1075) + 53);
+        ac += c;
+      }
+    }
+  }
+  if (lane < K) {
+    wsum1[warp][lane] = a1;
+    wsum2[warp][lane] = a2;
+    wcnt[warp][lane] = ac;
+  }
+  __syncthreads();
+  if (tid < K) {
+    MomPart p;
+    p.s1 = 0.0;
+    p.s2 = 0.0;
+    p.cnt = 0;
+    for (int w = 0; w < FT / 32; ++w) {
+      p.s1 += wsum1[w][tid];
+      p.s2 += wsum2[w][tid];
+      p.cnt += wcnt[w][tid];
+    }
+    p.pinf = infs[0][tid];
+    p.ninf = infs[1][tid];
+    parts[(row * chunks + chunk) * K + tid] = p;
+  }
+}
+
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) tiny_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                      long long m, int K, long long chunk_len, long long chunks,
+                                                      SelPart* __restrict__ parts) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned long long* bk = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][FT]
+  unsigned long long* bi = bk + K * FT;                                     // [K][FT]
+  __shared__ unsigned long long wk[FT / 32][kTinyK], wi[FT / 32][kTinyK];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len;
+  const long long c1 = min(m, c0 + chunk_len);
+  const bool is_idx = F == kFirst || F == kLast;
+  for (int k = 0; k < K; ++k) {
+    bk[k * FT + tid] = (F == kFirst) ? ~0ull : 0ull;
+    bi[k * FT + tid] = ~0ull;
+  }
+  const V* vr = values + row * m;
+  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1; base += static_cast<long long>(FT / 32) * kTileCols) {
+#pragma unroll 4
+    for (int j = 0; j < 16; ++j) {
+      const long long col = base + j * 32 + lane;
+      if (col >= c1) break;
+      const long long l = static_cast<long long>(labels[col]);
+      const V v = vr[col];
+      if (l < 0 || l >= K || is_nan(v)) continue;
+      const int slot = static_cast<int>(l) * FT + tid;
+      const unsigned long long c = static_cast<unsigned long long>(col);
+      if (F == kFirst) {
+        if (c < bk[slot]) bk[slot] = c;
+      } else if (F == kLast) {
+        if (c + 1 > bk[slot]) bk[slot] = c + 1;
+      } else {
+        const unsigned long long key = sel_key<F>(static_cast<double>(v));
+        if (key > bk[slot]) {  // columns arrive in increasing order: strict > keeps the first
+          bk[slot] = key;
+          bi[slot] = c;
+        }
+      }
+    }
+  }
+  // reduce lanes, then warps (fixed order)
+  for (int k = 0; k < K; ++k) {
+    unsigned long long key = bk[k * FT + tid], idx = bi[k * FT + tid];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+      const unsigned long long oi = __shfl_xor_sync(0xffffffffu, idx, o);
+      if (is_idx) {
+        key = (F == kFirst) ? min(key, ok) : max(key, ok);
+      } else if (better(ok, oi, key, idx)) {
+        key = ok;
+        idx = oi;
+      }
+    }
+    if (lane == 0) {
+      wk[warp][k] = key;
+      wi[warp][k] = idx;
+    }
+  }
+  __syncthreads();
+  if (tid < K) {
+    unsigned long long key = wk[0][tid], idx = wi[0][tid];
+    for (int w = 1; w < FT / 32; ++w) {
+      if (is_idx) {
+        key = (F == kFirst) ? min(key, wk[w][tid]) : max(key, wk[w][tid]);
+      } else if (better(wk[w][tid], wi[w][tid], key, idx)) {
+        key = wk[w][tid];
+        idx = wi[w][tid];
+      }
+    }
+    parts[(row * chunks + chunk) * K + tid] = SelPart{key, idx};
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// label histograms (shared by all rows)
+// ---------------------------------------------------------------------------------
+// per chunk (medium path): hist[chunk][k]
+template <typename L>
+__global__ void __launch_bounds__(FT) chunk_hist_kernel(const L* __restrict__ labels, long long m, int K,
+                                                        long long chunk_len, unsigned* __restrict__ hist) {
+  extern __shared__ unsigned hsm[];
+  const long long chunk = blockIdx.x;
+  for (int k = threadIdx.x; k < K; k += FT) hsm[k] = 0;
+  __syncthreads();
+  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
+  for (long long c = c0 + threadIdx.x; c < c1; c += FT) {
+    const long long l = static_cast<long long>(labels[c]);
+    if (l >= 0 && l < K) atomicAdd(&hsm[l], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < K; k += FT) hist[chunk * K + k] = hsm[k];
+}
+// whole row (large path): hist[k]
+template <typename L>
+__global__ void __launch_bounds__(FT) row_hist_kernel(const L* __restrict__ labels, long long m, long long K,
+                                                      unsigned* __restrict__ hist) {
+  const long long stride = static_cast<long long>(gridDim.x) * FT;
+  for (long long c = static_cast<long long>(blockIdx.x) * FT + threadIdx.x; c < m; c += stride) {
+    const long long l = static_cast<long long>(labels[c]);
+    if (l >= 0 && l < K) atomicAdd(&hist[l], 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// medium K: CTA-shared bins
+// ---------------------------------------------------------------------------------
+template <int F>
+NBG_HOST_DEVICE size_t mid_mom_bytes_per_bin() {
+  return (Need<F>::s1 ? 8 : 0) + (Need<F>::s2 ? 8 : 0) + (Need<F>::cnt ? 4 : 0) + ((Need<F>::s1 || Need<F>::s2) ? 4 : 0);
+}
+
+// A bin may hold at most 2^15 terms in the 48-bit format before it must be flushed.
+// The chunk's label histogram (known before the launch) bounds every bin's count, so
+// the CTA flushes only when some label is that frequent in the chunk.
+constexpr long long kMaxTermsPerFlush = 1ll << 15;
+
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) mid_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long m, int K, long long chunk_len, long long chunks,
+                                                     const unsigned* __restrict__ hist, MomPart* __restrict__ parts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool MOM = Need<F>::s1 || Need<F>::s2;
+  unsigned char* cur = smem_raw;
+  unsigned long long* b1 = reinterpret_cast<unsigned long long*>(cur);
+  if (Need<F>::s1) cur += static_cast<size_t>(K) * 8;
+  unsigned long long* b2 = reinterpret_cast<unsigned long long*>(cur);
+  if (Need<F>::s2) cur += static_cast<size_t>(K) * 8;
+  unsigned* nanc = reinterpret_cast<unsigned*>(cur);
+  if (Need<F>::cnt) cur += static_cast<size_t>(K) * 4;
+  int* infc = reinterpret_cast<int*>(cur);  // +1 per +inf, +65536 per -inf
+  __shared__ int emax_w[FT / 32];
+  __shared__ int scale_smem;
+  __shared__ unsigned maxhist_w[FT / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len;
+  const long long c1 = min(m, c0 + chunk_len);
+  MomPart* pr = parts + (row * chunks + chunk) * K;
+  unsigned hmax = 0;
+  for (int k = tid; k < K; k += FT) {
+    if (Need<F>::s1) b1[k] = 0;
+    if (Need<F>::s2) b2[k] = 0;
+    if (Need<F>::cnt) nanc[k] = 0;
+    if (MOM) infc[k] = 0;
+    pr[k] = MomPart{0.0, 0.0, 0, 0, 0};
+    hmax = max(hmax, hist[chunk * K + k]);
+  }
+  hmax = __reduce_max_sync(0xffffffffu, hmax);
+  if (lane == 0) maxhist_w[warp] = hmax;
+  if (tid == 0) scale_smem = 0;
+  __syncthreads();
+  hmax = 0;
+#pragma unroll
+  for (int w = 0; w < FT / 32; ++w) hmax = max(hmax, maxhist_w[w]);
+  // also bounded by 2^15 infinities per counter (they share one int)
+  const long long flush_len = (hmax <= kMaxTermsPerFlush) ? chunk_len : kMaxTermsPerFlush;
+  const V* vr = values + row * m;
+  for (long long sub = c0; sub < c1; sub += flush_len) {
+    const long long send = min(c1, sub + flush_len);
+    for (long long base = sub; base < send; base += kCtaCols) {
+      V v[8];
+      int lab[8];
+      int emax = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const long long col = base + j * FT + tid;
+        const bool in = col < send;
+        v[j] = in ? vr[col] : V(0);
+        const long long l = in ? static_cast<long long>(labels[col]) : -1;
+        const bool lv = l >= 0 && l < K;
+        if (lv && is_nan(v[j])) {
+          if (Need<F>::cnt) atomicAdd(&nanc[l], 1u);
+          lab[j] = -1;
+        } else {
+          lab[j] = lv ? static_cast<int>(l) : -1;
+        }
+        if (MOM && lab[j] >= 0) {
+          const double x = static_cast<double>(v[j]);
+          if (!is_inf_d(x) && !(Need<F>::varlike && sq_overflows(x))) emax = max(emax, bexp(x));
+        }
+      }
+      if (MOM) {
+        emax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
+        if (lane == 0) emax_w[warp] = emax;
+        __syncthreads();
+        int et = 0;
+#pragma unroll
+        for (int w = 0; w < FT / 32; ++w) et = max(et, emax_w[w]);
+        int E = scale_smem;
+        if (et > E) {  // the scale grows: shift what the bins hold (uniform branch)
+          if (E != 0) {
+            const int d = et - E;
+            for (int k = tid; k < K; k += FT) {
+              if (Need<F>::s1) b1[k] = static_cast<unsigned long long>(static_cast<long long>(b1[k]) >> min(d, 63));
+              if (Need<F>::s2) b2[k] = d >= 32 ? 0ull : (b2[k] >> (2 * d));
+            }
+          }
+          __syncthreads();
+          if (tid == 0) scale_smem = et;
+          E = et;
+        }
+        __syncthreads();
+        E = max(E, 1);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (lab[j] < 0) continue;
+          const double x = static_cast<double>(v[j]);
+          if (is_inf_d(x) || (Need<F>::varlike && sq_overflows(x))) {
+            atomicAdd(&infc[lab[j]], x > 0 ? 1 : 65536);
+            continue;
+          }
+          if (Need<F>::s1)
+            atomicAdd(&b1[lab[j]], static_cast<unsigned long long>(signed_of(x, aligned(x, E, 5))));
+          if (Need<F>::s2) atomicAdd(&b2[lab[j]], square_shift(aligned(x, E, 0), 58));
+        }
+      }
+    }
+    if (MOM) {
+      __syncthreads();
+      // flush into the CTA's own partial (float64)
+      const int E = max(scale_smem, 1);
+      for (int k = tid; k < K; k += FT) {
+        MomPart p = pr[k];
+        if (Need<F>::s1 && b1[k]) p.s1 += fix_to_double(static_cast<long long>(b1[k]), E - 1070);
+        if (Need<F>::s2 && b2[k]) p.s2 += fix_to_double(static_cast<long long>(b2[k]), 2 * (E - 1075) + 58);
+        p.pinf += infc[k] & 0xffff;
+        p.ninf += infc[k] >> 16;
+        pr[k] = p;
+        if (Need<F>::s1) b1[k] = 0;
+        if (Need<F>::s2) b2[k] = 0;
+        infc[k] = 0;
+      }
+      __syncthreads();
+      if (tid == 0) scale_smem = 0;
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (Need<F>::cnt) {
+    for (int k = tid; k < K; k += FT) pr[k].cnt = static_cast<long long>(hist[chunk * K + k]) - nanc[k];
+  }
+}
+
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long m, int K, long long chunk_len, long long chunks,
+                                                     SelPart* __restrict__ parts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* bins = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][2]
+  const int tid = threadIdx.x;
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len;
+  const long long c1 = min(m, c0 + chunk_len);
+  for (int k = tid; k < K; k += FT) {
+    bins[2 * k] = (F == kFirst) ? ~0ull : 0ull;
+    bins[2 * k + 1] = ~0ull;
+  }
+  __syncthreads();
+  const V* vr = values + row * m;
+  for (long long base = c0; base < c1; base += kCtaCols) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const long long col = base + j * FT + tid;
+      if (col >= c1) break;
+      const long long l = static_cast<long long>(labels[col]);
+      const V v = vr[col];
+      if (l < 0 || l >= K || is_nan(v)) continue;
+      const unsigned long long c = static_cast<unsigned long long>(col);
+      if (F == kFirst) atomicMin(&bins[2 * l], c);
+      else if (F == kLast) atomicMax(&bins[2 * l], c + 1);
+      else sel_update(&bins[2 * l], sel_key<F>(static_cast<double>(v)), c, true);
+    }
+  }
+  __syncthreads();
+  SelPart* pr = parts + (row * chunks + chunk) * K;
+  for (int k = tid; k < K; k += FT) pr[k] = SelPart{bins[2 * k], bins[2 * k + 1]};
+}
+
+// ---------------------------------------------------------------------------------
+// large K: per-row accumulators in global memory (kept in L2 by row-major CTA order)
+// ---------------------------------------------------------------------------------
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long m, long long K, long long chunk_len, long long chunks,
+                                                     double* __restrict__ acc1, double* __restrict__ acc2,
+                                                     unsigned* __restrict__ nanc) {
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
+  const V* vr = values + row * m;
+  double* r1 = acc1 + row * K;
+  double* r2 = acc2 + row * K;
+  unsigned* rn = nanc + row * K;
+  for (long long base = c0; base < c1; base += kCtaCols) {
+    V v[8];
+    long long lab[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const long long col = base + j * FT + threadIdx.x;
+      const bool in = col < c1;
+      v[j] = in ? vr[col] : V(0);
+      lab[j] = in ? static_cast<long long>(labels[col]) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const long long l = lab[j];
+      if (l < 0 || l >= K) continue;
+      if (is_nan(v[j])) {
+        if (Need<F>::cnt) atomicAdd(&rn[l], 1u);
+        continue;
+      }
+      const double x = static_cast<double>(v[j]);
+      if (Need<F>::s1) atomicAdd(&r1[l], x);
+      if (Need<F>::s2) atomicAdd(&r2[l], x * x);
+    }
+  }
+}
+
+__global__ void init_sel_kernel(unsigned long long* __restrict__ acc, long long n) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+    acc[2 * t] = 0ull;       // key 0 is below every real key
+    acc[2 * t + 1] = ~0ull;  // no index yet
+  }
+}
+
+template <int F, typename V, typename L>
+__global__ void __launch_bounds__(FT) big_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long m, long long K, long long chunk_len, long long chunks,
+                                                     unsigned long long* __restrict__ acc) {
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
+  const V* vr = values + row * m;
+  unsigned long long* ar = acc + row * K * 2;
+  for (long long base = c0; base < c1; base += kCtaCols) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const long long col = base + j * FT + threadIdx.x;
+      if (col >= c1) break;
+      const long long l = static_cast<long long>(labels[col]);
+      const V v = vr[col];
+      if (l < 0 || l >= K || is_nan(v)) continue;
+      const unsigned long long c = static_cast<unsigned long long>(col);
+      if (F == kFirst) atomicMin(&ar[2 * l], c);
+      else if (F == kLast) atomicMax(&ar[2 * l], c + 1);
+      else sel_update(&ar[2 * l], sel_key<F>(static_cast<double>(v)), c, false);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// finalisation: fold the partials over chunks (in chunk order) and write the output
+// ---------------------------------------------------------------------------------
+template <int F, typename O>
+NBG_DEVICE O finish_mom(double s1, double s2, long long cnt, int pinf, int ninf, long long ddof) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  if (F == kCount) return static_cast<O>(cnt);
+  if (F == kSum || F == kMean) {
+    double s = s1;
+    if (pinf && ninf) s = nan;
+    else if (pinf) s = inf;
+    else if (ninf) s = -inf;
+    if (F == kSum) return static_cast<O>(s);
+    return static_cast<O>(cnt == 0 ? nan : s / static_cast<double>(cnt));  // numbagg/grouped.py:22-27
+  }
+  if (F == kSumSq) return static_cast<O>((pinf || ninf) ? inf : s2);
+  // kVar / kStd, numbagg/grouped.py:170-176
+  const long long denom = cnt - ddof;
+  if (denom <= 0 || pinf || ninf) return static_cast<O>(nan);
+  double v = (s2 - (s1 * s1) / static_cast<double>(cnt)) / static_cast<double>(denom);
+  if (F == kStd) v = sqrt(v);
+  return static_cast<O>(v);
+}
+
+template <int F, typename O>
+__global__ void fold_mom_kernel(const MomPart* __restrict__ parts, O* __restrict__ out, long long rows, long long K,
+                                long long chunks, long long ddof) {
+  const long long total = rows * K;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long row = t / K, k = t - row * K;
+    double s1 = 0.0, s2 = 0.0;
+    long long cnt = 0;
+    int pinf = 0, ninf = 0;
+    for (long long c = 0; c < chunks; ++c) {
+      const MomPart p = parts[(row * chunks + c) * K + k];
+      s1 += p.s1;
+      s2 += p.s2;
+      cnt += p.cnt;
+      pinf += p.pinf;
+      ninf += p.ninf;
+    }
+    out[t] = finish_mom<F, O>(s1, s2, cnt, pinf, ninf, ddof);
+  }
+}
+
+template <int F, typename O>
+__global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
+                                      const unsigned* __restrict__ nanc, const unsigned* __restrict__ hist,
+                                      O* __restrict__ out, long long rows, long long K, long long ddof) {
+  const long long total = rows * K;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long k = t % K;
+    const double s1 = Need<F>::s1 ? acc1[t] : 0.0;
+    const double s2 = Need<F>::s2 ? acc2[t] : 0.0;
+    const long long cnt = Need<F>::cnt ? static_cast<long long>(hist[k]) - nanc[t] : 1;
+    // infinities are already in the float64 sums (inf + x, inf - inf = NaN)
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    O r;
+    if (F == kCount) r = static_cast<O>(cnt);
+    else if (F == kSum) r = static_cast<O>(s1);
+    else if (F == kSumSq) r = static_cast<O>(s2);
+    else if (F == kMean) r = static_cast<O>(cnt == 0 ? nan : s1 / static_cast<double>(cnt));
+    else {
+      const long long denom = cnt - ddof;
+      double v = denom <= 0 ? nan : (s2 - (s1 * s1) / static_cast<double>(cnt)) / static_cast<double>(denom);
+      if (F == kStd) v = sqrt(v);
+      r = static_cast<O>(v);
+    }
+    out[t] = r;
+  }
+}
+
+template <int F, typename V, typename O>
+NBG_DEVICE O finish_sel(unsigned long long key, unsigned long long idx, const V* vrow) {
+  if (F == kFirst) return key == ~0ull ? (IsFloat<O>::value ? nan_of<O>() : O(0)) : static_cast<O>(vrow[key]);
+  if (F == kLast) return key == 0ull ? nan_of<O>() : static_cast<O>(vrow[key - 1]);
+  if (idx == ~0ull) return nan_of<O>();
+  if (F == kArgMax || F == kArgMin) return static_cast<O>(idx);
+  return static_cast<O>(static_cast<double>(vrow[idx]));  // max / min via the float64 running value
+}
+
+template <int F, typename V, typename O>
+__global__ void fold_sel_kernel(const SelPart* __restrict__ parts, const V* __restrict__ values, O* __restrict__ out,
+                                long long rows, long long m, long long K, long long chunks, int stride_parts) {
+  const long long total = rows * K;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const bool is_idx = F == kFirst || F == kLast;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long row = t / K, k = t - row * K;
+    unsigned long long key = (F == kFirst) ? ~0ull : 0ull, idx = ~0ull;
+    for (long long c = 0; c < chunks; ++c) {
+      const SelPart p = parts[(row * chunks + c) * K + k];
+      if (is_idx) {
+        key = (F == kFirst) ? min(key, p.key) : max(key, p.key);
+      } else if (p.idx != ~0ull && better(p.key, p.idx, key, idx)) {
+        key = p.key;
+        idx = p.idx;
+      }
+    }
+    out[t] = finish_sel<F, V, O>(key, idx, values + row * m);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------
+struct FastPlan {
+  int strategy;  // 0 tiny, 1 medium, 2 large
+  long long chunks, chunk_len;
+};
+
+inline size_t mid_smem_bytes(int f, long long K) {
+  size_t per = 16;
+  switch (f) {
+    case kSum: per = mid_mom_bytes_per_bin<kSum>(); break;
+    case kCount: per = mid_mom_bytes_per_bin<kCount>(); break;
+    case kMean: per = mid_mom_bytes_per_bin<kMean>(); break;
+    case kVar: per = mid_mom_bytes_per_bin<kVar>(); break;
+    case kStd: per = mid_mom_bytes_per_bin<kStd>(); break;
+    case kSumSq: per = mid_mom_bytes_per_bin<kSumSq>(); break;
+    default: per = 16; break;
+  }
+  return static_cast<size_t>(K) * per;
+}
+
+inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
+  FastPlan p;
+  const long long sms = num_sms();
+  if (K <= kTinyK) {
+    p.strategy = 0;
+  } else if (mid_smem_bytes(f, K) <= 100 * 1024) {
+    p.strategy = 1;
+  } else {
+    p.strategy = 2;
+  }
+  long long target = p.strategy == 2 ? sms * 8 : sms * 4;  // CTAs per row (large) / per call
+  long long chunks = p.strategy == 2 ? target : (target + rows - 1) / max(rows, 1ll);
+  const long long unit = p.strategy == 0 ? static_cast<long long>(kTileCols) * (FT / 32) : kCtaCols;
+  long long min_len = unit;
+  if (p.strategy == 1) min_len = max(unit, 4 * K);  // amortise initialising / writing K bins
+  long long max_chunks = (m + min_len - 1) / min_len;
+  chunks = max(1ll, min(chunks, max_chunks));
+  long long len = (m + chunks - 1) / chunks;
+  len = ((len + unit - 1) / unit) * unit;
+  p.chunk_len = max(len, unit);
+  p.chunks = max(1ll, (m + p.chunk_len - 1) / p.chunk_len);
+  return p;
+}
+
+inline size_t fast_bytes(int f, long long rows, long long m, long long K) {
+  const FastPlan p = fast_plan(f, rows, m, K);
+  if (p.strategy == 2) {
+    if (is_moments(f)) return static_cast<size_t>(rows * K) * (8 + 8 + 4) + static_cast<size_t>(K) * 4 + 1024;
+    return static_cast<size_t>(rows * K) * 16 + 1024;
+  }
+  const size_t part = is_moments(f) ? sizeof(MomPart) : sizeof(SelPart);
+  size_t b = static_cast<size_t>(rows * p.chunks * K) * part + 1024;
+  if (p.strategy == 1 && is_moments(f)) b += static_cast<size_t>(p.chunks * K) * 4 + 256;
+  return b;
+}
+
+inline bool fast_path(int f, bool float_values) {
+  return (is_moments(f) && float_values) || is_select(f) || f == kFirst || f == kLast;
+}
+
+template <typename T>
+T* carve(unsigned char*& p, size_t count) {
+  p = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(p) + 255) & ~static_cast<size_t>(255));
+  T* r = reinterpret_cast<T*>(p);
+  p += count * sizeof(T);
+  return r;
+}
+
+inline int fin_grid(long long total) {
+  long long blocks = (total + 255) / 256;
+  const long long cap = static_cast<long long>(num_sms()) * 16;
+  return static_cast<int>(max(1ll, min(blocks, cap)));
+}
+
+// The default dynamic limit is 48 KiB minus the kernel's static shared memory (up to a
+// few KiB here), so the opt-in is needed from well below 48 KiB of dynamic bytes.
+template <typename K>
+void set_smem(K kern, size_t bytes) {
+  if (bytes > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+template <int F, typename V, typename L, typename O>
+int launch_fast(const V* values, const L* labels, O* out, long long rows, long long m, long long K, long long ddof,
+                void* ws, size_t ws_bytes, cudaStream_t s) {
+  const FastPlan p = fast_plan(F, rows, m, K);
+  if (!ws || ws_bytes < fast_bytes(F, rows, m, K)) return kWorkspaceTooSmall;
+  unsigned char* cur = static_cast<unsigned char*>(ws);
+  const long long nctas = rows * p.chunks;
+  if (p.strategy < 2 && nctas > 0x7fffffffll) return kUnsupported;
+  int launches = 0;
+  if (is_moments(F)) {
+    if (p.strategy == 0) {
+      MomPart* parts = carve<MomPart>(cur, rows * p.chunks * K);
+      const size_t smem = static_cast<size_t>(K) * FT * (8 + 8 + 4);
+      auto kern = tiny_mom_kernel<F, V, L>;
+      set_smem(kern, smem);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
+      launches = 2;
+    } else if (p.strategy == 1) {
+      MomPart* parts = carve<MomPart>(cur, rows * p.chunks * K);
+      unsigned* hist = carve<unsigned>(cur, p.chunks * K);
+      {  // per-chunk label histogram: valid counts, and the flush bound of the bins
+        auto hk = chunk_hist_kernel<L>;
+        set_smem(hk, static_cast<size_t>(K) * 4);
+        hk<<<static_cast<int>(p.chunks), FT, static_cast<size_t>(K) * 4, s>>>(labels, m, static_cast<int>(K), p.chunk_len, hist);
+        ++launches;
+      }
+      const size_t smem = mid_smem_bytes(F, K);
+      auto kern = mid_mom_kernel<F, V, L>;
+      set_smem(kern, smem);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, hist, parts);
+      fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
+      launches += 2;
+    } else {
+      double* acc1 = carve<double>(cur, rows * K);
+      double* acc2 = carve<double>(cur, Need<F>::s2 ? rows * K : 1);
+      unsigned* nanc = carve<unsigned>(cur, rows * K);
+      unsigned* hist = carve<unsigned>(cur, K);
+      if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(rows * K) * 8, s);
+      if (Need<F>::s2) cudaMemsetAsync(acc2, 0, static_cast<size_t>(rows * K) * 8, s);
+      if (Need<F>::cnt) {
+        cudaMemsetAsync(nanc, 0, static_cast<size_t>(rows * K) * 4, s);
+        cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
+        row_hist_kernel<L><<<fin_grid(m), FT, 0, s>>>(labels, m, K, hist);
+        ++launches;
+      }
+      big_mom_kernel<F, V, L><<<static_cast<int>(nctas), FT, 0, s>>>(values, labels, m, K, p.chunk_len, p.chunks, acc1, acc2, nanc);
+      big_mom_finish_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(acc1, acc2, nanc, hist, out, rows, K, ddof);
+      launches += 2;
+    }
+  } else {
+    if (p.strategy == 0) {
+      SelPart* parts = carve<SelPart>(cur, rows * p.chunks * K);
+      const size_t smem = static_cast<size_t>(K) * FT * 16;
+      auto kern = tiny_sel_kernel<F, V, L>;
+      set_smem(kern, smem);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, values, out, rows, m, K, p.chunks, 1);
+      launches = 2;
+    } else if (p.strategy == 1) {
+      SelPart* parts = carve<SelPart>(cur, rows * p.chunks * K);
+      const size_t smem = static_cast<size_t>(K) * 16;
+      auto kern = mid_sel_kernel<F, V, L>;
+      set_smem(kern, smem);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, values, out, rows, m, K, p.chunks, 1);
+      launches = 2;
+    } else {
+      unsigned long long* acc = carve<unsigned long long>(cur, rows * K * 2);
+      // key 0 / index ~0 means "empty" (first: key ~0)
+      if (F == kFirst) cudaMemsetAsync(acc, 0xff, static_cast<size_t>(rows * K) * 16, s);
+      else if (F == kLast) cudaMemsetAsync(acc, 0, static_cast<size_t>(rows * K) * 16, s);
+      else init_sel_kernel<<<fin_grid(rows * K), 256, 0, s>>>(acc, rows * K);
+      big_sel_kernel<F, V, L><<<static_cast<int>(nctas), FT, 0, s>>>(values, labels, m, K, p.chunk_len, p.chunks, acc);
+      fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(reinterpret_cast<const SelPart*>(acc), values, out,
+                                                                    rows, m, K, 1, 1);
+      launches = (F == kFirst || F == kLast) ? 2 : 3;
+    }
+  }
+  note_launches(launches);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
+
+}  // namespace grouped
+}  // namespace nbg
+
+// ---------------------------------------------------------------------------------
+// exported entry points of the fast paths
+// ---------------------------------------------------------------------------------
+namespace nbg {
+namespace grouped {
+size_t fast_bytes_query(int f, long long rows, long long m, long long K) {
+  if (!(is_moments(f) || is_select(f) || f == kFirst || f == kLast)) return 0;
+  return fast_bytes(f, rows, m, K);
+}
+}  // namespace grouped
+}  // namespace nbg
+
+using namespace nbg;
+using namespace nbg::grouped;
+
+namespace {
+template <int F, typename V, typename L, typename O>
+int group_fast_entry(const V* values, const L* labels, O* out, long long rows, long long m, long long K,
+                     long long ddof, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (rows < 0 || m < 0 || K < 0) return kInvalidArgument;
+  if (rows == 0 || K == 0) return kOk;
+  if (!out || (m > 0 && (!values || !labels))) return kInvalidArgument;
+  if (K > 0x7fffffffll) return kUnsupported;
+  // m == 0 still runs: one chunk of no columns writes every output's empty value
+  return launch_fast<F, V, L, O>(values, labels, out, rows, m, K, ddof, ws, ws_bytes, s);
+}
+}  // namespace
+
+extern "C" {
+#define NBG_GFAST_ONE(NAME, FC, V, VS, O, L, LS)                                               \
+  int nbg_group_##NAME##_##VS##_##LS(const V* values, const L* labels, O* out, long long rows,  \
+                                     long long m, long long num_labels, long long ddof, void* ws, \
+                                     size_t ws_bytes, void* stream) {                          \
+    return group_fast_entry<FC, V, L, O>(values, labels, out, rows, m, num_labels, ddof, ws,    \
+                                         ws_bytes, static_cast<cudaStream_t>(stream));         \
+  }
+#define NBG_GFAST_LABELS(NAME, FC, V, VS, O) \
+  NBG_GFAST_ONE(NAME, FC, V, VS, O, int, i32) NBG_GFAST_ONE(NAME, FC, V, VS, O, long long, i64)
+#define NBG_GFAST_FLOAT(NAME, FC)                 \
+  NBG_GFAST_LABELS(NAME, FC, double, f64, double) \
+  NBG_GFAST_LABELS(NAME, FC, float, f32, float)
+#define NBG_GFAST_ALL(NAME, FC)                          \
+  NBG_GFAST_FLOAT(NAME, FC)                              \
+  NBG_GFAST_LABELS(NAME, FC, int, i32, int)              \
+  NBG_GFAST_LABELS(NAME, FC, long long, i64, long long)
+
+NBG_GFAST_FLOAT(nansum, kSum)
+NBG_GFAST_FLOAT(nancount, kCount)
+NBG_GFAST_FLOAT(nanmean, kMean)
+NBG_GFAST_FLOAT(nanvar, kVar)
+NBG_GFAST_FLOAT(nanstd, kStd)
+NBG_GFAST_FLOAT(nansum_of_squares, kSumSq)
+NBG_GFAST_ALL(nanargmax, kArgMax)
+NBG_GFAST_ALL(nanargmin, kArgMin)
+NBG_GFAST_ALL(nanmax, kMax)
+NBG_GFAST_ALL(nanmin, kMin)
+NBG_GFAST_ALL(nanfirst, kFirst)
+NBG_GFAST_ALL(nanlast, kLast)
+}  // extern "C"
