@@ -58,6 +58,7 @@ def parse_args(argv=None):
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cols", type=int, default=COLS, help="columns (smaller for quick runs)")
+    p.add_argument("--only", default=None, help="regex: time only the calls whose key matches (profiling)")
     return p.parse_args(argv)
 
 
@@ -350,6 +351,10 @@ def run_ours(args):
     rows, cols = ROWS, args.cols
     values, labels, fill = make_inputs(rows, cols, device)
     calls = calls_and_bytes(rows, cols)
+    if args.only:
+        import re
+
+        calls = [c for c in calls if re.search(args.only, c[0])]
     torch.cuda.synchronize(device)
 
     for _ in range(args.warmup):

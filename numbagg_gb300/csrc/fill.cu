@@ -35,21 +35,37 @@ struct LastOp {
 
 constexpr int NT = 256;
 
+// One CTA scans tiles of NT * K positions; warp w owns the K * 32 consecutive
+// positions starting at w * K * 32, in K groups of 32 (lane l of group j holds
+// position j * 32 + l, so every load and store of a warp is one contiguous run).
+// Within a group, lane l's last valid position is the highest set bit of the group's
+// valid ballot at or below l; a group without one inherits the warp's running
+// (position, value).  Positions before the warp's first valid element need the carry
+// from earlier warps or tiles and are written after it is known: the warp's carry-in
+// is the last valid element of the earlier warps of the tile, else the tile's
+// exclusive prefix from decoupled look-back.  A tile holding a valid element already
+// knows its inclusive prefix (its own last valid element) and publishes it at once,
+// and it looks back only if its first position is NaN.
 template <typename T, bool REVERSE, int K>
-__global__ void __launch_bounds__(NT) fill_kernel(const T* __restrict__ a, T* __restrict__ out,
+__global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T* __restrict__ out,
                                                   long long rows, long long n, long long limit,
                                                   long long tiles_per_row, void* ws_base,
                                                   size_t ws_bytes) {
-  constexpr long long TILE = static_cast<long long>(NT) * K;
-  __shared__ long long warp_idx[NT / 32];
-  __shared__ double warp_val[NT / 32];
-  __shared__ Last carry_smem;
+  constexpr long long WSPAN = 32LL * K;
+  constexpr long long TILE = WSPAN * (NT / 32);
+  constexpr int NW = NT / 32;
+  __shared__ long long w_idx[NW];
+  __shared__ double w_val[NW];
+  __shared__ int w_first[NW];
+  __shared__ long long in_idx[NW];
+  __shared__ double in_val[NW];
   __shared__ long long tile_smem;
   const long long total_tiles = rows * tiles_per_row;
   Workspace ws = make_workspace(ws_base, ws_bytes);
   const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const unsigned lane_le = 0xffffffffu >> (31 - lane);
+  const T nan = quiet_nan(T(0));
 
   for (;;) {
     if (threadIdx.x == 0) tile_smem = claim_tile(ws.hdr);
@@ -59,106 +75,99 @@ __global__ void __launch_bounds__(NT) fill_kernel(const T* __restrict__ a, T* __
     const TileCoord tc = tile_coord(tile, rows);
     const long long row = tc.row, chunk = tc.chunk;
     // scan-order position q maps to array position i = q (ffill) or n-1-q (bfill)
-    const long long q0 = chunk * TILE + static_cast<long long>(threadIdx.x) * K;
+    const long long wq0 = chunk * TILE + static_cast<long long>(warp) * WSPAN;
     const T* ar = a + row * n;
     T* orow = out + row * n;
 
     T v[K];
-    long long li = -1;
-    double lv = 0.0;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long q = q0 + k;
-      const long long i = REVERSE ? n - 1 - q : q;
-      v[k] = q < n ? ar[i] : T(0);
-      if (q < n && !is_nan(v[k])) {
-        li = q;
-        lv = static_cast<double>(v[k]);
-      }
+    for (int j = 0; j < K; ++j) {
+      const long long q = wq0 + j * 32 + lane;
+      v[j] = q < n ? __ldcs(ar + (REVERSE ? n - 1 - q : q)) : T(0);
     }
-    // warp inclusive scan of (li, lv): later valid wins
-    long long si = li;
-    double sv = lv;
+    long long cidx = -1;  // the warp's running last valid position (uniform)
+    T cval = T(0);
+    int first = static_cast<int>(WSPAN);
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const long long ui = __shfl_up_sync(0xffffffffu, si, d);
-      const double uv = __shfl_up_sync(0xffffffffu, sv, d);
-      if (lane >= d && si < 0) {
-        si = ui;
-        sv = uv;
+    for (int j = 0; j < K; ++j) {
+      const long long qb = wq0 + j * 32;
+      const long long q = qb + lane;
+      const bool valid = q < n && !is_nan(v[j]);
+      const unsigned msk = __ballot_sync(0xffffffffu, valid);
+      const unsigned mle = msk & lane_le;
+      const int src = mle ? 31 - __clz(mle) : lane;
+      const T sv = __shfl_sync(0xffffffffu, v[j], src);
+      long long ei = cidx;
+      T ev = cval;
+      if (mle) {
+        ei = qb + src;
+        ev = sv;
       }
-    }
-    if (lane == 31) {
-      warp_idx[warp] = si;
-      warp_val[warp] = sv;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      long long wi = lane < NT / 32 ? warp_idx[lane] : -1;
-      double wv = lane < NT / 32 ? warp_val[lane] : 0.0;
-#pragma unroll
-      for (int d = 1; d < NT / 32; d <<= 1) {
-        const long long ui = __shfl_up_sync(0xffffffffu, wi, d);
-        const double uv = __shfl_up_sync(0xffffffffu, wv, d);
-        if (lane >= d && wi < 0) {
-          wi = ui;
-          wv = uv;
-        }
+      if (msk) {
+        const int top = 31 - __clz(msk);
+        cval = __shfl_sync(0xffffffffu, v[j], top);
+        cidx = qb + top;
+        if (first == static_cast<int>(WSPAN)) first = j * 32 + __ffs(msk) - 1;
       }
-      if (lane < NT / 32) {
-        warp_idx[lane] = wi;
-        warp_val[lane] = wv;
-      }
+      if (q < n && ei >= 0) orow[REVERSE ? n - 1 - q : q] = (q - ei <= limit) ? ev : nan;
     }
-    __syncthreads();
-    // exclusive prefix for this thread: previous lane's inclusive value, else the
-    // previous warp's inclusive value
-    long long ei = __shfl_up_sync(0xffffffffu, si, 1);
-    double ev = __shfl_up_sync(0xffffffffu, sv, 1);
     if (lane == 0) {
-      ei = -1;
-      ev = 0.0;
+      w_idx[warp] = cidx;
+      w_val[warp] = static_cast<double>(cval);
+      w_first[warp] = first;
     }
-    if (ei < 0 && warp > 0) {
-      ei = warp_idx[warp - 1];
-      ev = warp_val[warp - 1];
-    }
+    __syncthreads();
     if (warp == 0) {
-      const Last agg{warp_idx[NT / 32 - 1], warp_val[NT / 32 - 1]};
-      if (chunk == 0) {
-        if (lane == 0) {
-          if (tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
-          carry_smem = Last{-1, 0.0};
+      long long li = -1;
+      double lv = 0.0;
+      if (lane == 0) {
+        for (int w = 0; w < NW; ++w) {  // carry-in of every warp from the earlier warps
+          in_idx[w] = li;
+          in_val[w] = lv;
+          if (w_idx[w] >= 0) {
+            li = w_idx[w];
+            lv = w_val[w];
+          }
         }
-      } else {
+      }
+      li = __shfl_sync(0xffffffffu, li, 0);
+      lv = __shfl_sync(0xffffffffu, lv, 0);
+      const Last agg{li, lv};
+      Last excl{-1, 0.0};
+      if (chunk == 0) {
+        if (lane == 0 && tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
+      } else if (agg.idx >= 0) {
+        if (lane == 0) publish(ws, tile, epoch, kStatePrefix, agg);
+        if (w_first[0] != 0) {  // leading NaNs: the carry from earlier tiles is needed
+          __syncwarp();
+          bool ok;
+          excl = warp_lookback<Last>(ws, tile, chunk, rows, epoch, LastOp(), ok);
+        }
+      } else {  // no valid element: the inclusive prefix is the exclusive one
         if (lane == 0) publish(ws, tile, epoch, kStateAggregate, agg);
         __syncwarp();
         bool ok;
-        const Last carry = warp_lookback<Last>(ws, tile, chunk, rows, epoch, LastOp(), ok);
-        if (lane == 0) {
-          publish(ws, tile, epoch, kStatePrefix, LastOp().combine(carry, agg));
-          carry_smem = carry;
+        excl = warp_lookback<Last>(ws, tile, chunk, rows, epoch, LastOp(), ok);
+        if (lane == 0) publish(ws, tile, epoch, kStatePrefix, excl);
+      }
+      if (lane == 0) {
+        for (int w = 0; w < NW; ++w) {
+          if (in_idx[w] < 0) {
+            in_idx[w] = excl.idx;
+            in_val[w] = excl.val;
+          }
         }
       }
     }
     __syncthreads();
-    if (ei < 0) {
-      ei = carry_smem.idx;
-      ev = carry_smem.val;
+    // the positions before the warp's first valid element
+    if (first > 0) {
+      const long long ci = in_idx[warp];
+      const T cv = static_cast<T>(in_val[warp]);
+      const long long qend = min(wq0 + first, n);
+      for (long long q = wq0 + lane; q < qend; q += 32)
+        orow[REVERSE ? n - 1 - q : q] = (ci >= 0 && q - ci <= limit) ? cv : nan;
     }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long q = q0 + k;
-      if (q >= n) break;
-      const long long i = REVERSE ? n - 1 - q : q;
-      if (!is_nan(v[k])) {
-        ei = q;
-        ev = static_cast<double>(v[k]);
-      }
-      const double r = (ei >= 0 && q - ei <= limit) ? ev : nan;
-      orow[i] = static_cast<T>(r);
-    }
-    __syncthreads();
   }
   if (threadIdx.x == 0) finish_cta(ws.hdr);
 }

@@ -30,6 +30,7 @@
 // compare-and-swap issued only when the element improves on the current pair.
 // first / last are a minimum / maximum of the column index.  All of these are exact.
 #include "grouped_common.cuh"
+#include "fixed128.cuh"
 
 namespace nbg {
 namespace grouped {
@@ -88,20 +89,11 @@ NBG_DEVICE long long signed_of(double x, unsigned long long mag) {
 // v * 2^L as a double
 NBG_DEVICE double fix_to_double(long long v, int L) { return scalbn(__ll2double_rn(v), L); }
 
-// Fixed-point formats.  tiny: value = aligned(x, E, 0) * 2^(E - 1075)     (53 bits)
-//                              square = (a*a) >> 53  * 2^(2(E - 1075) + 53)
-//                       medium: value = aligned(x, E, 5) * 2^(E - 1070)     (48 bits)
-//                              square = (a*a) >> 58  * 2^(2(E - 1075) + 58)
-// where a = aligned(x, E, 0).  Headroom: 10 bits (tiny), 15 bits (medium).
+// Fixed-point format of the medium path:
+//   value = aligned(x, E, 5) * 2^(E - 1070)                (48 bits)
+//   square = (a*a) >> 58  * 2^(2(E - 1075) + 58)            a = aligned(x, E, 0)
+// with 15 bits of headroom.
 
-template <typename V>
-NBG_DEVICE bool valid_value(V v) { return !is_nan(v); }
-
-template <int F>
-NBG_DEVICE unsigned long long sel_key(double x) {
-  const unsigned long long k = order_key_ieee(x);
-  return (F == kArgMin || F == kMin) ? ~k : k;
-}
 NBG_DEVICE bool better(unsigned long long k1, unsigned long long i1, unsigned long long k2, unsigned long long i2) {
   return k1 > k2 || (k1 == k2 && i1 < i2);
 }
@@ -142,90 +134,199 @@ NBG_DEVICE void sel_update(unsigned long long* addr, unsigned long long key, uns
 }
 
 // ---------------------------------------------------------------------------------
+// values taken apart with integer instructions only.  This GPU's FP64 pipe accepts a
+// warp instruction every 16 cycles whatever the number of active lanes, so nothing
+// that runs per element (or per bin and tile) may use it.
+// ---------------------------------------------------------------------------------
+struct Dec {
+  unsigned long long m;  // integer mantissa: value = m * 2^(e - 1075)
+  int e;                 // biased float64 exponent (1 for zeros and subnormals)
+  bool neg;              // sign bit
+  bool special;          // infinity or NaN
+};
+NBG_DEVICE Dec decomp(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int eb = static_cast<int>((b >> 52) & 0x7ff);
+  Dec d;
+  d.m = (b & 0x000fffffffffffffull) | (eb ? 0x0010000000000000ull : 0ull);
+  d.e = eb ? eb : 1;
+  d.neg = (b >> 63) != 0;
+  d.special = eb == 0x7ff;
+  return d;
+}
+// a float32 restated exactly in the float64 format
+NBG_DEVICE Dec decomp(float x) {
+  const unsigned b = static_cast<unsigned>(__float_as_int(x));
+  const int eb = static_cast<int>((b >> 23) & 0xff);
+  Dec d;
+  d.m = static_cast<unsigned long long>((b & 0x7fffffu) | (eb ? 0x800000u : 0u)) << 29;
+  d.e = eb ? eb + 896 : 897;
+  d.neg = (b >> 31) != 0;
+  d.special = eb == 0xff;
+  return d;
+}
+// integer values reach the moment kernels only through the generic path; these keep
+// the templates well-formed
+NBG_DEVICE Dec decomp(int x) { return decomp(static_cast<double>(x)); }
+NBG_DEVICE Dec decomp(long long x) { return decomp(static_cast<double>(x)); }
+
+// Order key of a value for the selection functions: a < b (compared as float64, the
+// reference's comparison) <=> key(a) < key(b), -0.0 and +0.0 equal, and no key is 0
+// (0 marks an empty bin).
+NBG_DEVICE unsigned long long value_key(double v) { return order_key_ieee(v); }
+NBG_DEVICE unsigned long long value_key(float v) {
+  unsigned b = static_cast<unsigned>(__float_as_int(v));
+  if ((b << 1) == 0) b = 0;
+  return (b >> 31) ? static_cast<unsigned long long>(~b) : static_cast<unsigned long long>(b | 0x80000000u);
+}
+NBG_DEVICE unsigned long long value_key(int v) {  // exact as float64; offset binary, plus one
+  return static_cast<unsigned long long>(static_cast<unsigned>(v) ^ 0x80000000u) + 1ull;
+}
+NBG_DEVICE unsigned long long value_key(long long v) { return order_key_ieee(static_cast<double>(v)); }
+template <int F, typename V>
+NBG_DEVICE unsigned long long sel_key_of(V v) {
+  const unsigned long long k = value_key(v);
+  return (F == kArgMin || F == kMin) ? ~k : k;
+}
+
+// ---------------------------------------------------------------------------------
 // tiny K: lane-private bins
 // ---------------------------------------------------------------------------------
+// A warp keeps a scale exponent E, the largest biased exponent among the finite values
+// it has met (it only grows), and every lane keeps its own K bins in shared memory:
+//   value  x   -> +-(m >> (E - e + d1))          LSB 2^(E + d1 - 1075)
+//   square x^2 -> (m*m) >> (2(E - e) + d2)        LSB 2^(2E + d2 - 2150)
+// d1, d2 come from the host: with n the number of elements one lane can meet in its
+// chunk (< 2^lg), d1 = max(0, lg - 10) and d2 = 43 + lg, so a lane's sums stay below
+// 2^63.  When E grows, each lane shifts its own bins down.  Bits below the LSB are
+// truncated: at most 2^-(52 - d1) of the largest value the warp met, per term.
+// At the end of the chunk the lanes' bins are summed exactly (128-bit) per warp and
+// rounded once to float64.
 template <int F, typename V, typename L>
-__global__ void __launch_bounds__(FT) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                      long long m, int K, long long chunk_len, long long chunks,
-                                                      MomPart* __restrict__ parts) {
-  extern __shared__ unsigned char smem_raw[];
+__global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                         long long rows, long long m, int K, long long chunk_len,
+                                                         long long chunks, int d1, int d2,
+                                                         MomPart* __restrict__ parts) {
+  constexpr bool S1 = Need<F>::s1, S2 = Need<F>::s2, CNT = Need<F>::cnt, VL = Need<F>::varlike;
+  constexpr bool MOM = S1 || S2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   long long* b1 = reinterpret_cast<long long*>(smem_raw);  // [K][FT]
-  long long* b2 = b1 + K * FT;                              // [K][FT]
-  int* bc = reinterpret_cast<int*>(b2 + K * FT);            // [K][FT]
+  unsigned long long* b2 = reinterpret_cast<unsigned long long*>(smem_raw + (S1 ? K * FT * 8 : 0));
+  int* bc = reinterpret_cast<int*>(smem_raw + (S1 ? K * FT * 8 : 0) + (S2 ? K * FT * 8 : 0));
   __shared__ double wsum1[FT / 32][kTinyK], wsum2[FT / 32][kTinyK];
-  __shared__ long long wcnt[FT / 32][kTinyK];
+  __shared__ int wcnt[FT / 32][kTinyK];
   __shared__ int infs[2][kTinyK];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  // chunk-major order: the CTAs in flight share the chunks of labels they read
+  const long long chunk = blockIdx.x / rows, row = blockIdx.x - chunk * rows;
   const long long c0 = chunk * chunk_len;
   const long long c1 = min(m, c0 + chunk_len);
   for (int k = 0; k < K; ++k) {
-    b1[k * FT + tid] = 0;
-    b2[k * FT + tid] = 0;
-    bc[k * FT + tid] = 0;
+    if (S1) b1[k * FT + tid] = 0;
+    if (S2) b2[k * FT + tid] = 0;
+    if (CNT) bc[k * FT + tid] = 0;
   }
   if (tid < 2 * kTinyK) infs[tid / kTinyK][tid % kTinyK] = 0;
   __syncthreads();
   const V* vr = values + row * m;
-  double a1 = 0.0, a2 = 0.0;
-  long long ac = 0;
-  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1; base += static_cast<long long>(FT / 32) * kTileCols) {
+  int E = 0;  // the warp's scale (uniform across the warp)
+  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
+       base += static_cast<long long>(FT / 32) * kTileCols) {
     V v[16];
     int lab[16];
-    int emax = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const long long col = base + j * 32 + lane;
       const bool in = col < c1;
-      v[j] = in ? vr[col] : V(0);
-      const long long l = in ? static_cast<long long>(labels[col]) : -1;
-      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
-      if (lab[j] >= 0) {
-        const double x = static_cast<double>(v[j]);
-        if (!is_inf_d(x) && !(Need<F>::varlike && sq_overflows(x))) emax = max(emax, bexp(x));
+      v[j] = in ? __ldcs(vr + col) : V(0);
+      const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
+      lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
+    }
+    int emax = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (is_nan(v[j])) lab[j] = -1;
+      if (MOM) {
+        const Dec d = decomp(v[j]);
+        if (lab[j] >= 0 && !d.special && !(VL && d.e >= 1023 + 512)) emax = max(emax, d.e);
       }
     }
-    const int E = max(1, static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax))));
+    if (MOM) {
+      const int Et = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
+      if (Et > E) {  // uniform: the warp's scale grows
+        if (E > 0) {
+          const int dd = Et - E;
+          for (int k = 0; k < K; ++k) {
+            const int slot = k * FT + tid;
+            if (S1) b1[slot] = dd >= 63 ? (b1[slot] < 0 ? -1ll : 0ll) : (b1[slot] >> dd);
+            if (S2) b2[slot] = 2 * dd >= 64 ? 0ull : (b2[slot] >> (2 * dd));
+          }
+        }
+        E = Et;
+      }
+    }
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       if (lab[j] < 0) continue;
-      const double x = static_cast<double>(v[j]);
       const int slot = lab[j] * FT + tid;
-      if (Need<F>::cnt) bc[slot] += 1;
-      if (is_inf_d(x) || (Need<F>::varlike && sq_overflows(x))) {
-        atomicAdd(&infs[x > 0 ? 0 : 1][lab[j]], 1);
+      if (CNT) bc[slot] += 1;
+      if (!MOM) continue;
+      const Dec d = decomp(v[j]);
+      if (d.special || (VL && d.e >= 1023 + 512)) {  // infinity, or a square that overflows
+        atomicAdd(&infs[d.neg ? 1 : 0][lab[j]], 1);
         continue;
       }
-      const unsigned long long a = aligned(x, E, 0);
-      if (Need<F>::s1) b1[slot] += signed_of(x, a);
-      if (Need<F>::s2) b2[slot] += static_cast<long long>(square_shift(a, 53));
-    }
-    __syncwarp();
-    // flush the tile: sum the lanes' bins, lane k adds bin k as float64
-    for (int k = 0; k < K; ++k) {
-      const int slot = k * FT + tid;
-      long long s1 = 0, s2 = 0;
-      int c = 0;
-      if (Need<F>::s1) { s1 = b1[slot]; b1[slot] = 0; }
-      if (Need<F>::s2) { s2 = b2[slot]; b2[slot] = 0; }
-      if (Need<F>::cnt) { c = bc[slot]; bc[slot] = 0; }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        if (Need<F>::s1) s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        if (Need<F>::s2) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        if (Need<F>::cnt) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (S1) {
+        const int sh = E - d.e + d1;
+        const unsigned long long a = sh >= 64 ? 0ull : (d.m >> sh);
+        b1[slot] += d.neg ? -static_cast<long long>(a) : static_cast<long long>(a);
       }
-      if (lane == k) {
-        if (Need<F>::s1 && s1) a1 += fix_to_double(s1, E - 1075);
-        if (Need<F>::s2 && s2) a2 += fix_to_double(s2, 2 * (E - 1075) + 53);
-        ac += c;
+      if (S2) {
+        const int sh = 2 * (E - d.e) + d2;  // >= d2 >= 43
+        unsigned long long q = 0ull;
+        if (sh < 106) {
+          const unsigned long long lo = d.m * d.m, hi = __umul64hi(d.m, d.m);
+          q = sh >= 64 ? (hi >> (sh - 64)) : ((hi << (64 - sh)) | (lo >> sh));
+        }
+        b2[slot] += q;
       }
     }
   }
-  if (lane < K) {
-    wsum1[warp][lane] = a1;
-    wsum2[warp][lane] = a2;
-    wcnt[warp][lane] = ac;
+  // lanes' bins -> exact warp sums -> float64 at the warp's scale
+  for (int k = 0; k < K; ++k) {
+    const int slot = k * FT + tid;
+    if (S1) {
+      const long long x = b1[slot];
+      unsigned long long lo = static_cast<unsigned long long>(x);
+      long long hi = x < 0 ? -1ll : 0ll;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o);
+        const long long ohi = __shfl_xor_sync(0xffffffffu, hi, o);
+        const unsigned long long nlo = lo + olo;
+        hi = hi + ohi + (nlo < lo ? 1 : 0);
+        lo = nlo;
+      }
+      if (lane == 0)
+        wsum1[warp][k] = fx::to_double((static_cast<fx::i128>(hi) << 64) + static_cast<fx::i128>(lo), E + d1 - 1075);
+    }
+    if (S2) {
+      unsigned long long lo = b2[slot], hi = 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o);
+        const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, hi, o);
+        const unsigned long long nlo = lo + olo;
+        hi = hi + ohi + (nlo < lo ? 1ull : 0ull);
+        lo = nlo;
+      }
+      if (lane == 0)
+        wsum2[warp][k] = fx::to_double(static_cast<fx::i128>((static_cast<fx::u128>(hi) << 64) | lo), 2 * E + d2 - 2150);
+    }
+    if (CNT) {
+      const int c = static_cast<int>(__reduce_add_sync(0xffffffffu, static_cast<unsigned>(bc[slot])));
+      if (lane == 0) wcnt[warp][k] = c;
+    }
   }
   __syncthreads();
   if (tid < K) {
@@ -233,10 +334,10 @@ __global__ void __launch_bounds__(FT) tiny_mom_kernel(const V* __restrict__ valu
     p.s1 = 0.0;
     p.s2 = 0.0;
     p.cnt = 0;
-    for (int w = 0; w < FT / 32; ++w) {
-      p.s1 += wsum1[w][tid];
-      p.s2 += wsum2[w][tid];
-      p.cnt += wcnt[w][tid];
+    for (int w = 0; w < FT / 32; ++w) {  // fixed order: deterministic
+      if (S1) p.s1 += wsum1[w][tid];
+      if (S2) p.s2 += wsum2[w][tid];
+      if (CNT) p.cnt += wcnt[w][tid];
     }
     p.pinf = infs[0][tid];
     p.ninf = infs[1][tid];
@@ -245,40 +346,48 @@ __global__ void __launch_bounds__(FT) tiny_mom_kernel(const V* __restrict__ valu
 }
 
 template <int F, typename V, typename L>
-__global__ void __launch_bounds__(FT) tiny_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                      long long m, int K, long long chunk_len, long long chunks,
-                                                      SelPart* __restrict__ parts) {
-  extern __shared__ unsigned char smem_raw[];
+__global__ void __launch_bounds__(FT, 2) tiny_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                         long long rows, long long m, int K, long long chunk_len,
+                                                         long long chunks, SelPart* __restrict__ parts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* bk = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][FT]
   unsigned long long* bi = bk + K * FT;                                     // [K][FT]
   __shared__ unsigned long long wk[FT / 32][kTinyK], wi[FT / 32][kTinyK];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long chunk = blockIdx.x / rows, row = blockIdx.x - chunk * rows;
   const long long c0 = chunk * chunk_len;
   const long long c1 = min(m, c0 + chunk_len);
-  const bool is_idx = F == kFirst || F == kLast;
+  constexpr bool is_idx = F == kFirst || F == kLast;
   for (int k = 0; k < K; ++k) {
     bk[k * FT + tid] = (F == kFirst) ? ~0ull : 0ull;
     bi[k * FT + tid] = ~0ull;
   }
   const V* vr = values + row * m;
-  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1; base += static_cast<long long>(FT / 32) * kTileCols) {
-#pragma unroll 4
+  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
+       base += static_cast<long long>(FT / 32) * kTileCols) {
+    V v[16];
+    int lab[16];
+#pragma unroll
     for (int j = 0; j < 16; ++j) {
       const long long col = base + j * 32 + lane;
-      if (col >= c1) break;
-      const long long l = static_cast<long long>(labels[col]);
-      const V v = vr[col];
-      if (l < 0 || l >= K || is_nan(v)) continue;
-      const int slot = static_cast<int>(l) * FT + tid;
-      const unsigned long long c = static_cast<unsigned long long>(col);
+      const bool in = col < c1;
+      v[j] = in ? __ldcs(vr + col) : V(0);
+      const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
+      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
+    }
+    // a lane meets its columns in increasing order
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (lab[j] < 0) continue;
+      const int slot = lab[j] * FT + tid;
+      const unsigned long long c = static_cast<unsigned long long>(base + j * 32 + lane);
       if (F == kFirst) {
-        if (c < bk[slot]) bk[slot] = c;
+        if (bk[slot] == ~0ull) bk[slot] = c;
       } else if (F == kLast) {
-        if (c + 1 > bk[slot]) bk[slot] = c + 1;
+        bk[slot] = c + 1;
       } else {
-        const unsigned long long key = sel_key<F>(static_cast<double>(v));
-        if (key > bk[slot]) {  // columns arrive in increasing order: strict > keeps the first
+        const unsigned long long key = sel_key_of<F>(v[j]);
+        if (key > bk[slot]) {  // strict: the earlier column keeps a tie
           bk[slot] = key;
           bi[slot] = c;
         }
@@ -364,139 +473,150 @@ constexpr long long kMaxTermsPerFlush = 1ll << 15;
 
 template <int F, typename V, typename L>
 __global__ void __launch_bounds__(FT) mid_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                     long long m, int K, long long chunk_len, long long chunks,
-                                                     const unsigned* __restrict__ hist, MomPart* __restrict__ parts) {
+                                                     long long rows, long long m, int K, long long chunk_len,
+                                                     long long chunks, const unsigned* __restrict__ hist,
+                                                     MomPart* __restrict__ parts) {
+  constexpr bool S1 = Need<F>::s1, S2 = Need<F>::s2, CNT = Need<F>::cnt, VL = Need<F>::varlike;
+  constexpr bool MOM = S1 || S2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr bool MOM = Need<F>::s1 || Need<F>::s2;
   unsigned char* cur = smem_raw;
   unsigned long long* b1 = reinterpret_cast<unsigned long long*>(cur);
-  if (Need<F>::s1) cur += static_cast<size_t>(K) * 8;
+  if (S1) cur += static_cast<size_t>(K) * 8;
   unsigned long long* b2 = reinterpret_cast<unsigned long long*>(cur);
-  if (Need<F>::s2) cur += static_cast<size_t>(K) * 8;
+  if (S2) cur += static_cast<size_t>(K) * 8;
   unsigned* nanc = reinterpret_cast<unsigned*>(cur);
-  if (Need<F>::cnt) cur += static_cast<size_t>(K) * 4;
-  int* infc = reinterpret_cast<int*>(cur);  // +1 per +inf, +65536 per -inf
-  __shared__ int emax_w[FT / 32];
-  __shared__ int scale_smem;
-  __shared__ unsigned maxhist_w[FT / 32];
+  if (CNT) cur += static_cast<size_t>(K) * 4;
+  unsigned* infc = reinterpret_cast<unsigned*>(cur);  // +1 per +inf, +65536 per -inf
+  __shared__ unsigned red_w[FT / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  // chunk-major order: the CTAs in flight share the chunks of labels they read
+  const long long chunk = blockIdx.x / rows, row = blockIdx.x - chunk * rows;
   const long long c0 = chunk * chunk_len;
   const long long c1 = min(m, c0 + chunk_len);
   MomPart* pr = parts + (row * chunks + chunk) * K;
   unsigned hmax = 0;
   for (int k = tid; k < K; k += FT) {
-    if (Need<F>::s1) b1[k] = 0;
-    if (Need<F>::s2) b2[k] = 0;
-    if (Need<F>::cnt) nanc[k] = 0;
+    if (S1) b1[k] = 0;
+    if (S2) b2[k] = 0;
+    if (CNT) nanc[k] = 0;
     if (MOM) infc[k] = 0;
     pr[k] = MomPart{0.0, 0.0, 0, 0, 0};
     hmax = max(hmax, hist[chunk * K + k]);
   }
   hmax = __reduce_max_sync(0xffffffffu, hmax);
-  if (lane == 0) maxhist_w[warp] = hmax;
-  if (tid == 0) scale_smem = 0;
+  if (lane == 0) red_w[warp] = hmax;
   __syncthreads();
   hmax = 0;
 #pragma unroll
-  for (int w = 0; w < FT / 32; ++w) hmax = max(hmax, maxhist_w[w]);
-  // also bounded by 2^15 infinities per counter (they share one int)
+  for (int w = 0; w < FT / 32; ++w) hmax = max(hmax, red_w[w]);
+  __syncthreads();
+  // also bounds the infinities per counter (2^15 of each fit in the packed word)
   const long long flush_len = (hmax <= kMaxTermsPerFlush) ? chunk_len : kMaxTermsPerFlush;
   const V* vr = values + row * m;
+  int E = 0;  // the CTA's scale, the same in every thread
   for (long long sub = c0; sub < c1; sub += flush_len) {
     const long long send = min(c1, sub + flush_len);
     for (long long base = sub; base < send; base += kCtaCols) {
       V v[8];
       int lab[8];
-      int emax = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const long long col = base + j * FT + tid;
         const bool in = col < send;
-        v[j] = in ? vr[col] : V(0);
-        const long long l = in ? static_cast<long long>(labels[col]) : -1;
-        const bool lv = l >= 0 && l < K;
-        if (lv && is_nan(v[j])) {
-          if (Need<F>::cnt) atomicAdd(&nanc[l], 1u);
+        v[j] = in ? __ldcs(vr + col) : V(0);
+        const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
+        lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
+      }
+      int emax = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (lab[j] >= 0 && is_nan(v[j])) {
+          if (CNT) atomicAdd(&nanc[lab[j]], 1u);
           lab[j] = -1;
-        } else {
-          lab[j] = lv ? static_cast<int>(l) : -1;
         }
-        if (MOM && lab[j] >= 0) {
-          const double x = static_cast<double>(v[j]);
-          if (!is_inf_d(x) && !(Need<F>::varlike && sq_overflows(x))) emax = max(emax, bexp(x));
+        if (MOM) {
+          const Dec d = decomp(v[j]);
+          if (lab[j] >= 0 && !d.special && !(VL && d.e >= 1023 + 512)) emax = max(emax, d.e);
         }
       }
       if (MOM) {
-        emax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
-        if (lane == 0) emax_w[warp] = emax;
-        __syncthreads();
-        int et = 0;
+        if (__syncthreads_or(emax > E)) {  // the CTA's scale grows: shift what the bins hold
+          const int wm = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
+          if (lane == 0) red_w[warp] = static_cast<unsigned>(wm);
+          __syncthreads();
+          int En = E;
 #pragma unroll
-        for (int w = 0; w < FT / 32; ++w) et = max(et, emax_w[w]);
-        int E = scale_smem;
-        if (et > E) {  // the scale grows: shift what the bins hold (uniform branch)
-          if (E != 0) {
-            const int d = et - E;
+          for (int w = 0; w < FT / 32; ++w) En = max(En, static_cast<int>(red_w[w]));
+          if (E > 0) {
+            const int dd = En - E;
             for (int k = tid; k < K; k += FT) {
-              if (Need<F>::s1) b1[k] = static_cast<unsigned long long>(static_cast<long long>(b1[k]) >> min(d, 63));
-              if (Need<F>::s2) b2[k] = d >= 32 ? 0ull : (b2[k] >> (2 * d));
+              if (S1) {
+                const long long x = static_cast<long long>(b1[k]);
+                b1[k] = static_cast<unsigned long long>(dd >= 63 ? (x < 0 ? -1ll : 0ll) : (x >> dd));
+              }
+              if (S2) b2[k] = 2 * dd >= 64 ? 0ull : (b2[k] >> (2 * dd));
             }
           }
+          E = En;
           __syncthreads();
-          if (tid == 0) scale_smem = et;
-          E = et;
         }
-        __syncthreads();
-        E = max(E, 1);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           if (lab[j] < 0) continue;
-          const double x = static_cast<double>(v[j]);
-          if (is_inf_d(x) || (Need<F>::varlike && sq_overflows(x))) {
-            atomicAdd(&infc[lab[j]], x > 0 ? 1 : 65536);
+          const Dec d = decomp(v[j]);
+          if (d.special || (VL && d.e >= 1023 + 512)) {  // infinity, or a square that overflows
+            atomicAdd(&infc[lab[j]], d.neg ? 65536u : 1u);
             continue;
           }
-          if (Need<F>::s1)
-            atomicAdd(&b1[lab[j]], static_cast<unsigned long long>(signed_of(x, aligned(x, E, 5))));
-          if (Need<F>::s2) atomicAdd(&b2[lab[j]], square_shift(aligned(x, E, 0), 58));
+          if (S1) {
+            const int sh = E - d.e + 5;
+            const unsigned long long a = sh >= 64 ? 0ull : (d.m >> sh);
+            atomicAdd(&b1[lab[j]], d.neg ? (~a + 1ull) : a);
+          }
+          if (S2) {
+            const int sh = 2 * (E - d.e) + 58;
+            unsigned long long q = 0ull;
+            if (sh < 106) {
+              const unsigned long long lo = d.m * d.m, hi = __umul64hi(d.m, d.m);
+              q = sh >= 64 ? (hi >> (sh - 64)) : ((hi << (64 - sh)) | (lo >> sh));
+            }
+            atomicAdd(&b2[lab[j]], q);
+          }
         }
       }
     }
     if (MOM) {
       __syncthreads();
       // flush into the CTA's own partial (float64)
-      const int E = max(scale_smem, 1);
       for (int k = tid; k < K; k += FT) {
         MomPart p = pr[k];
-        if (Need<F>::s1 && b1[k]) p.s1 += fix_to_double(static_cast<long long>(b1[k]), E - 1070);
-        if (Need<F>::s2 && b2[k]) p.s2 += fix_to_double(static_cast<long long>(b2[k]), 2 * (E - 1075) + 58);
-        p.pinf += infc[k] & 0xffff;
-        p.ninf += infc[k] >> 16;
+        if (S1 && b1[k]) p.s1 += fx::to_double(static_cast<fx::i128>(static_cast<long long>(b1[k])), E + 5 - 1075);
+        if (S2 && b2[k]) p.s2 += fx::to_double(static_cast<fx::i128>(b2[k]), 2 * E + 58 - 2150);
+        p.pinf += static_cast<int>(infc[k] & 0xffffu);
+        p.ninf += static_cast<int>(infc[k] >> 16);
         pr[k] = p;
-        if (Need<F>::s1) b1[k] = 0;
-        if (Need<F>::s2) b2[k] = 0;
+        if (S1) b1[k] = 0;
+        if (S2) b2[k] = 0;
         infc[k] = 0;
       }
-      __syncthreads();
-      if (tid == 0) scale_smem = 0;
+      E = 0;
       __syncthreads();
     }
   }
   __syncthreads();
-  if (Need<F>::cnt) {
+  if (CNT) {
     for (int k = tid; k < K; k += FT) pr[k].cnt = static_cast<long long>(hist[chunk * K + k]) - nanc[k];
   }
 }
 
 template <int F, typename V, typename L>
 __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                     long long m, int K, long long chunk_len, long long chunks,
-                                                     SelPart* __restrict__ parts) {
+                                                     long long rows, long long m, int K, long long chunk_len,
+                                                     long long chunks, SelPart* __restrict__ parts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* bins = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][2]
   const int tid = threadIdx.x;
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long chunk = blockIdx.x / rows, row = blockIdx.x - chunk * rows;
   const long long c0 = chunk * chunk_len;
   const long long c1 = min(m, c0 + chunk_len);
   for (int k = tid; k < K; k += FT) {
@@ -506,17 +626,28 @@ __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ value
   __syncthreads();
   const V* vr = values + row * m;
   for (long long base = c0; base < c1; base += kCtaCols) {
+    V v[8];
+    int lab[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const long long col = base + j * FT + tid;
-      if (col >= c1) break;
-      const long long l = static_cast<long long>(labels[col]);
-      const V v = vr[col];
-      if (l < 0 || l >= K || is_nan(v)) continue;
-      const unsigned long long c = static_cast<unsigned long long>(col);
-      if (F == kFirst) atomicMin(&bins[2 * l], c);
-      else if (F == kLast) atomicMax(&bins[2 * l], c + 1);
-      else sel_update(&bins[2 * l], sel_key<F>(static_cast<double>(v)), c, true);
+      const bool in = col < c1;
+      v[j] = in ? __ldcs(vr + col) : V(0);
+      const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
+      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (lab[j] < 0) continue;
+      const unsigned long long c = static_cast<unsigned long long>(base + j * FT + tid);
+      unsigned long long* b = &bins[2 * lab[j]];
+      if (F == kFirst) {
+        if (c < *reinterpret_cast<volatile unsigned long long*>(b)) atomicMin(b, c);
+      } else if (F == kLast) {
+        atomicMax(b, c + 1);
+      } else {
+        sel_update(b, sel_key_of<F>(v[j]), c, true);
+      }
     }
   }
   __syncthreads();
@@ -590,7 +721,7 @@ __global__ void __launch_bounds__(FT) big_sel_kernel(const V* __restrict__ value
       const unsigned long long c = static_cast<unsigned long long>(col);
       if (F == kFirst) atomicMin(&ar[2 * l], c);
       else if (F == kLast) atomicMax(&ar[2 * l], c + 1);
-      else sel_update(&ar[2 * l], sel_key<F>(static_cast<double>(v)), c, false);
+      else sel_update(&ar[2 * l], sel_key_of<F>(v), c, false);
     }
   }
 }
@@ -733,7 +864,8 @@ inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
   } else {
     p.strategy = 2;
   }
-  long long target = p.strategy == 2 ? sms * 8 : sms * 4;  // CTAs per row (large) / per call
+  // large: CTAs per row; tiny / medium: CTAs per call, four waves of two CTAs per SM
+  long long target = sms * 8;
   long long chunks = p.strategy == 2 ? target : (target + rows - 1) / max(rows, 1ll);
   const long long unit = p.strategy == 0 ? static_cast<long long>(kTileCols) * (FT / 32) : kCtaCols;
   long long min_len = unit;
@@ -796,10 +928,16 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   if (is_moments(F)) {
     if (p.strategy == 0) {
       MomPart* parts = carve<MomPart>(cur, rows * p.chunks * K);
-      const size_t smem = static_cast<size_t>(K) * FT * (8 + 8 + 4);
+      const size_t smem = static_cast<size_t>(K) * FT * ((Need<F>::s1 ? 8 : 0) + (Need<F>::s2 ? 8 : 0) + (Need<F>::cnt ? 4 : 0));
+      // headroom of the lanes' fixed-point sums (see tiny_mom_kernel)
+      const long long per_lane = ((p.chunk_len + kTileCols * (FT / 32) - 1) / (kTileCols * (FT / 32))) * 16;
+      int lg = 0;
+      while ((1ll << lg) < per_lane) ++lg;
+      const int d1 = lg > 10 ? lg - 10 : 0, d2 = 43 + lg;
       auto kern = tiny_mom_kernel<F, V, L>;
       set_smem(kern, smem);
-      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
+                                                     d1, d2, parts);
       fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
       launches = 2;
     } else if (p.strategy == 1) {
@@ -814,7 +952,8 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       const size_t smem = mid_smem_bytes(F, K);
       auto kern = mid_mom_kernel<F, V, L>;
       set_smem(kern, smem);
-      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, hist, parts);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
+                                                     hist, parts);
       fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
       launches += 2;
     } else {
@@ -840,7 +979,8 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       const size_t smem = static_cast<size_t>(K) * FT * 16;
       auto kern = tiny_sel_kernel<F, V, L>;
       set_smem(kern, smem);
-      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
+                                                     parts);
       fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, values, out, rows, m, K, p.chunks, 1);
       launches = 2;
     } else if (p.strategy == 1) {
@@ -848,7 +988,8 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       const size_t smem = static_cast<size_t>(K) * 16;
       auto kern = mid_sel_kernel<F, V, L>;
       set_smem(kern, smem);
-      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, m, static_cast<int>(K), p.chunk_len, p.chunks, parts);
+      kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
+                                                     parts);
       fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, values, out, rows, m, K, p.chunks, 1);
       launches = 2;
     } else {

@@ -48,6 +48,9 @@ enum Status : int {
 // ---------------------------------------------------------------------------------
 // bit-level predicates
 // ---------------------------------------------------------------------------------
+// the quiet NaN numpy writes (np.nan), in the type of the argument
+NBG_DEVICE double quiet_nan(double) { return __longlong_as_double(0x7ff8000000000000ll); }
+NBG_DEVICE float quiet_nan(float) { return __int_as_float(0x7fc00000); }
 NBG_DEVICE bool is_nan(double x) {
   const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
   return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
