@@ -47,6 +47,15 @@ NBG_API size_t nbg_workspace_header_bytes(void);
 NBG_API int nbg_workspace_error(void* ws, int* code, unsigned* tile, void* stream);
 /* Number of kernels this library has launched in the process (all devices). */
 NBG_API unsigned long long nbg_launch_count(void);
+
+/* Deterministic mode (no reference counterpart: numbagg is sequential and always
+ * reproducible; this mirrors torch.use_deterministic_algorithms).  When on, every
+ * call either runs an algorithm whose result bits do not depend on scheduling, or
+ * returns NBG_UNSUPPORTED: float group sums / means / variances with more labels than
+ * fit the shared-memory bins (several thousand) have only a float64-atomic
+ * implementation.  Off by default; process-wide. */
+NBG_API void nbg_set_deterministic(int on);
+NBG_API int nbg_get_deterministic(void);
 /* Test hook for failure detection: one bounded wait on a status nothing publishes. */
 NBG_API int nbg_debug_lookback_timeout(void* ws, size_t ws_bytes, int spin_limit, void* stream);
 

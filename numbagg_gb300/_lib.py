@@ -38,6 +38,9 @@ c_d = ctypes.c_double
 c_i = ctypes.c_int
 
 
+UNSUPPORTED = 5
+
+
 class NbgError(RuntimeError):
     """A CUDA-side failure reported by the C ABI."""
 
@@ -50,6 +53,8 @@ def _declare(lib: ctypes.CDLL) -> None:
 
     sig("nbg_version", c_i)
     sig("nbg_launch_count", ctypes.c_ulonglong)
+    sig("nbg_set_deterministic", None, c_i)
+    sig("nbg_get_deterministic", c_i)
     sig("nbg_status_string", ctypes.c_char_p, c_i)
     sig("nbg_workspace_header_bytes", c_sz)
     sig("nbg_workspace_error", c_i, c_vp, ctypes.POINTER(c_i), ctypes.POINTER(ctypes.c_uint), c_vp)

@@ -7,12 +7,17 @@ using namespace nbg;
 
 namespace nbg {
 static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<int> g_deterministic{0};
 void note_launches(int n) { g_launches.fetch_add(static_cast<unsigned long long>(n), std::memory_order_relaxed); }
+bool deterministic_mode() { return g_deterministic.load(std::memory_order_relaxed) != 0; }
 }  // namespace nbg
 
 extern "C" {
 
 unsigned long long nbg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+void nbg_set_deterministic(int on) { g_deterministic.store(on ? 1 : 0, std::memory_order_relaxed); }
+int nbg_get_deterministic(void) { return g_deterministic.load(std::memory_order_relaxed); }
 
 int nbg_version(void) { return 10000; }  // 1.0.0
 

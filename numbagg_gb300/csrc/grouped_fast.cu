@@ -656,42 +656,97 @@ __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ value
 }
 
 // ---------------------------------------------------------------------------------
-// large K: per-row accumulators in global memory (kept in L2 by row-major CTA order)
+// large K: float64 reductions into L2-resident accumulators, rows in blocks
 // ---------------------------------------------------------------------------------
-template <int F, typename V, typename L>
-__global__ void __launch_bounds__(FT) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                     long long m, long long K, long long chunk_len, long long chunks,
-                                                     double* __restrict__ acc1, double* __restrict__ acc2,
-                                                     unsigned* __restrict__ nanc) {
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
-  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
-  const V* vr = values + row * m;
-  double* r1 = acc1 + row * K;
-  double* r2 = acc2 + row * K;
-  unsigned* rn = nanc + row * K;
-  for (long long base = c0; base < c1; base += kCtaCols) {
-    V v[8];
-    long long lab[8];
+// Rows are taken RB at a time and the accumulators of a row block are laid out label
+// by label, acc[k][r] for the block's RB rows, so the RB values of one column (one
+// label) land in RB consecutive words.  A warp loads RB rows x 32 columns with the
+// lanes along the columns (whole cache lines), passes them through a padded shared
+// stage, and reduces with lane l on row l % RB and column group l / RB: the RB lanes
+// of a group reduce into one contiguous span, which the L2 serves several times
+// faster than RB scattered words.  CTAs run row block after row block and RB is
+// chosen so that a block's accumulators fit comfortably in L2.  The order of the
+// float64 reductions is not fixed, so sums may differ in the last bits from run to
+// run; counts and selections are exact.
+constexpr int kBigT = 16;  // loads in flight per lane
+
+NBG_HOST_DEVICE long long big_tile_cols(int rb) { return 32LL * (kBigT / rb) * (FT / 32); }
+
+template <typename V, int RB>
+struct BigStage {  // per warp: U sub-tiles of RB rows x 32 columns, rows padded
+  static constexpr int U = kBigT / RB;
+  static constexpr int P = RB == 1 ? 32 : 32 + 16 / RB;  // conflict-free transposed reads
+  V s[FT / 32][U][RB][P];
+};
+
+// Loads RB rows x 32U columns of the row block (lanes along the columns) and calls
+// f(u, v, l, live) for lane (r = lane % RB, g = lane / RB) on the RB elements it
+// reduces of each sub-tile u: value v of row r, label l of its column (-1 past c1).
+template <typename V, typename L, int RB, typename Fn>
+NBG_DEVICE void big_tiles(const V* __restrict__ values, const L* __restrict__ labels, long long rows, long long m,
+                          long long rb, long long c0, long long c1, BigStage<V, RB>& st, Fn&& f) {
+  constexpr int U = BigStage<V, RB>::U, G = 32 / RB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = lane % RB, g = lane / RB;
+  const long long row0 = rb * RB;
+  for (long long cbase = c0 + static_cast<long long>(warp) * 32 * U; cbase < c1;
+       cbase += static_cast<long long>(FT / 32) * 32 * U) {
+    V x[U][RB];
+    long long lab[U];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const long long col = base + j * FT + threadIdx.x;
+    for (int u = 0; u < U; ++u) {
+      const long long col = cbase + u * 32 + lane;
       const bool in = col < c1;
-      v[j] = in ? vr[col] : V(0);
-      lab[j] = in ? static_cast<long long>(labels[col]) : -1;
-    }
+      lab[u] = in ? static_cast<long long>(__ldg(labels + col)) : -1;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const long long l = lab[j];
-      if (l < 0 || l >= K) continue;
-      if (is_nan(v[j])) {
-        if (Need<F>::cnt) atomicAdd(&rn[l], 1u);
-        continue;
+      for (int rr = 0; rr < RB; ++rr)
+        x[u][rr] = (in && row0 + rr < rows) ? __ldcs(values + (row0 + rr) * m + col) : V(0);
+    }
+    if (RB == 1) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) f(u, x[u][0], lab[u], cbase + u * 32 + lane);
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int rr = 0; rr < RB; ++rr) st.s[warp][u][rr][lane] = x[u][rr];
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+          const int c = i * G + g;
+          const long long l = __shfl_sync(0xffffffffu, lab[u], c);
+          f(u, st.s[warp][u][r][c], l, cbase + u * 32 + c);
+        }
       }
-      const double x = static_cast<double>(v[j]);
-      if (Need<F>::s1) atomicAdd(&r1[l], x);
-      if (Need<F>::s2) atomicAdd(&r2[l], x * x);
+      __syncwarp();
     }
   }
+}
+
+template <int F, typename V, typename L, int RB>
+__global__ void __launch_bounds__(FT) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long rows, long long m, long long K, long long chunk_len,
+                                                     long long chunks, double* __restrict__ acc1,
+                                                     double* __restrict__ acc2, unsigned* __restrict__ nanc) {
+  __shared__ BigStage<V, RB> st;
+  const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
+  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
+  const int r = (threadIdx.x & 31) % RB;
+  const bool live = rb * RB + r < rows;
+  const long long off = rb * K * RB + r;  // accumulator of (label l, row r): off + l * RB
+  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st, [&](int, V v, long long l, long long) {
+    if (!live || l < 0 || l >= K) return;
+    const long long a = off + l * RB;
+    if (is_nan(v)) {
+      if (Need<F>::cnt) atomicAdd(&nanc[a], 1u);
+      return;
+    }
+    const double x = static_cast<double>(v);
+    if (Need<F>::s1) atomicAdd(&acc1[a], x);
+    if (Need<F>::s2) atomicAdd(&acc2[a], x * x);
+  });
 }
 
 __global__ void init_sel_kernel(unsigned long long* __restrict__ acc, long long n) {
@@ -702,28 +757,28 @@ __global__ void init_sel_kernel(unsigned long long* __restrict__ acc, long long 
   }
 }
 
-template <int F, typename V, typename L>
+template <int F, typename V, typename L, int RB>
 __global__ void __launch_bounds__(FT) big_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                     long long m, long long K, long long chunk_len, long long chunks,
-                                                     unsigned long long* __restrict__ acc) {
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+                                                     long long rows, long long m, long long K, long long chunk_len,
+                                                     long long chunks, unsigned long long* __restrict__ acc) {
+  __shared__ BigStage<V, RB> st;
+  const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
   const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
-  const V* vr = values + row * m;
-  unsigned long long* ar = acc + row * K * 2;
-  for (long long base = c0; base < c1; base += kCtaCols) {
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const long long col = base + j * FT + threadIdx.x;
-      if (col >= c1) break;
-      const long long l = static_cast<long long>(labels[col]);
-      const V v = vr[col];
-      if (l < 0 || l >= K || is_nan(v)) continue;
-      const unsigned long long c = static_cast<unsigned long long>(col);
-      if (F == kFirst) atomicMin(&ar[2 * l], c);
-      else if (F == kLast) atomicMax(&ar[2 * l], c + 1);
-      else sel_update(&ar[2 * l], sel_key_of<F>(v), c, false);
+  const int r = (threadIdx.x & 31) % RB;
+  const bool live = rb * RB + r < rows;
+  const long long off = rb * K * RB + r;
+  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st, [&](int, V v, long long l, long long col) {
+    if (!live || l < 0 || l >= K || is_nan(v)) return;
+    const unsigned long long c = static_cast<unsigned long long>(col);
+    unsigned long long* p = acc + 2 * (off + l * RB);
+    if (F == kFirst) {
+      if (c < __ldcg(p)) atomicMin(p, c);
+    } else if (F == kLast) {
+      atomicMax(p, c + 1);
+    } else {
+      sel_update(p, sel_key_of<F>(v), c, false);
     }
-  }
+  });
 }
 
 // ---------------------------------------------------------------------------------
@@ -773,31 +828,34 @@ __global__ void fold_mom_kernel(const MomPart* __restrict__ parts, O* __restrict
   }
 }
 
-template <int F, typename O>
+// accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]
+template <int F, typename O, int RB>
 __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
                                       const unsigned* __restrict__ nanc, const unsigned* __restrict__ hist,
                                       O* __restrict__ out, long long rows, long long K, long long ddof) {
-  const long long total = rows * K;
+  const long long total = (rows + RB - 1) / RB * K * RB;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
-    const long long k = t % K;
+    const long long rb = t / (K * RB), rem = t - rb * K * RB;
+    const long long k = rem / RB, row = rb * RB + (rem - k * RB);
+    if (row >= rows) continue;
     const double s1 = Need<F>::s1 ? acc1[t] : 0.0;
     const double s2 = Need<F>::s2 ? acc2[t] : 0.0;
     const long long cnt = Need<F>::cnt ? static_cast<long long>(hist[k]) - nanc[t] : 1;
     // infinities are already in the float64 sums (inf + x, inf - inf = NaN)
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    O r;
-    if (F == kCount) r = static_cast<O>(cnt);
-    else if (F == kSum) r = static_cast<O>(s1);
-    else if (F == kSumSq) r = static_cast<O>(s2);
-    else if (F == kMean) r = static_cast<O>(cnt == 0 ? nan : s1 / static_cast<double>(cnt));
+    O res;
+    if (F == kCount) res = static_cast<O>(cnt);
+    else if (F == kSum) res = static_cast<O>(s1);
+    else if (F == kSumSq) res = static_cast<O>(s2);
+    else if (F == kMean) res = static_cast<O>(cnt == 0 ? nan : s1 / static_cast<double>(cnt));
     else {
       const long long denom = cnt - ddof;
       double v = denom <= 0 ? nan : (s2 - (s1 * s1) / static_cast<double>(cnt)) / static_cast<double>(denom);
       if (F == kStd) v = sqrt(v);
-      r = static_cast<O>(v);
+      res = static_cast<O>(v);
     }
-    out[t] = r;
+    out[row * K + k] = res;
   }
 }
 
@@ -808,6 +866,19 @@ NBG_DEVICE O finish_sel(unsigned long long key, unsigned long long idx, const V*
   if (idx == ~0ull) return nan_of<O>();
   if (F == kArgMax || F == kArgMin) return static_cast<O>(idx);
   return static_cast<O>(static_cast<double>(vrow[idx]));  // max / min via the float64 running value
+}
+
+template <int F, typename V, typename O, int RB>
+__global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ acc, const V* __restrict__ values,
+                                      O* __restrict__ out, long long rows, long long m, long long K) {
+  const long long total = (rows + RB - 1) / RB * K * RB;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long rb = t / (K * RB), rem = t - rb * K * RB;
+    const long long k = rem / RB, row = rb * RB + (rem - k * RB);
+    if (row >= rows) continue;
+    out[row * K + k] = finish_sel<F, V, O>(acc[2 * t], acc[2 * t + 1], values + row * m);
+  }
 }
 
 template <int F, typename V, typename O>
@@ -837,8 +908,25 @@ __global__ void fold_sel_kernel(const SelPart* __restrict__ parts, const V* __re
 // ---------------------------------------------------------------------------------
 struct FastPlan {
   int strategy;  // 0 tiny, 1 medium, 2 large
-  long long chunks, chunk_len;
+  long long chunks, chunk_len;  // large: chunks per row block
+  int rb;                       // large: rows per block (1, 4 or 8)
+  long long blocks;             // large: row blocks
 };
+
+// Rows per block of the large path: as many as 16, as long as the block's
+// accumulators (K x RB x the bytes a bin keeps) stay within 64 MB of the L2, and no
+// more than the rows rounded up to a power of two.
+inline int big_rows_per_block(int f, long long rows, long long K) {
+  size_t per = 16;  // selection: (key, index)
+  if (is_moments(f)) {
+    per = 4;  // NaN count (count / mean / var / std; kept for the others too)
+    if (f == kSum || f == kMean || f == kVar || f == kStd) per += 8;
+    if (f == kVar || f == kStd || f == kSumSq) per += 8;
+  }
+  int rb = 16;
+  while (rb > 1 && (rb / 2 >= rows || static_cast<size_t>(K) * rb * per > (64ull << 20))) rb /= 2;
+  return rb;
+}
 
 inline size_t mid_smem_bytes(int f, long long K) {
   size_t per = 16;
@@ -859,15 +947,25 @@ inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
   const long long sms = num_sms();
   if (K <= kTinyK) {
     p.strategy = 0;
+  } else if (is_moments(f) && !deterministic_mode()) {
+    p.strategy = 2;  // float64 reductions in L2 beat shared-memory 64-bit atomics
   } else if (mid_smem_bytes(f, K) <= 100 * 1024) {
     p.strategy = 1;
   } else {
     p.strategy = 2;
   }
-  // large: CTAs per row; tiny / medium: CTAs per call, four waves of two CTAs per SM
-  long long target = sms * 8;
+  p.rb = 1;
+  p.blocks = rows;
+  if (p.strategy == 2) {
+    p.rb = big_rows_per_block(f, rows, K);
+    p.blocks = (rows + p.rb - 1) / p.rb;
+  }
+  // large: CTAs per row block (four per SM); tiny / medium: CTAs per call, four
+  // waves of two CTAs per SM
+  long long target = p.strategy == 2 ? sms * 4 : sms * 8;
   long long chunks = p.strategy == 2 ? target : (target + rows - 1) / max(rows, 1ll);
-  const long long unit = p.strategy == 0 ? static_cast<long long>(kTileCols) * (FT / 32) : kCtaCols;
+  const long long unit = p.strategy == 0 ? static_cast<long long>(kTileCols) * (FT / 32)
+                                         : (p.strategy == 1 ? kCtaCols : big_tile_cols(p.rb));
   long long min_len = unit;
   if (p.strategy == 1) min_len = max(unit, 4 * K);  // amortise initialising / writing K bins
   long long max_chunks = (m + min_len - 1) / min_len;
@@ -882,8 +980,9 @@ inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
 inline size_t fast_bytes(int f, long long rows, long long m, long long K) {
   const FastPlan p = fast_plan(f, rows, m, K);
   if (p.strategy == 2) {
-    if (is_moments(f)) return static_cast<size_t>(rows * K) * (8 + 8 + 4) + static_cast<size_t>(K) * 4 + 1024;
-    return static_cast<size_t>(rows * K) * 16 + 1024;
+    const size_t slots = static_cast<size_t>(p.blocks * p.rb * K);
+    if (is_moments(f)) return slots * (8 + 8 + 4) + static_cast<size_t>(K) * 4 + 1024;
+    return slots * 16 + 1024;
   }
   const size_t part = is_moments(f) ? sizeof(MomPart) : sizeof(SelPart);
   size_t b = static_cast<size_t>(rows * p.chunks * K) * part + 1024;
@@ -916,6 +1015,44 @@ void set_smem(K kern, size_t bytes) {
   if (bytes > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
 }
 
+template <int F, typename V, typename L, typename O, int RB>
+int launch_big_mom(const V* values, const L* labels, O* out, long long rows, long long m, long long K, long long ddof,
+                   const FastPlan& p, unsigned char*& cur, cudaStream_t s) {
+  const long long slots = p.blocks * RB * K;
+  double* acc1 = carve<double>(cur, slots);
+  double* acc2 = carve<double>(cur, Need<F>::s2 ? slots : 1);
+  unsigned* nanc = carve<unsigned>(cur, slots);
+  unsigned* hist = carve<unsigned>(cur, K);
+  int launches = 0;
+  if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * 8, s);
+  if (Need<F>::s2) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
+  if (Need<F>::cnt) {
+    cudaMemsetAsync(nanc, 0, static_cast<size_t>(slots) * 4, s);
+    cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
+    row_hist_kernel<L><<<fin_grid(m), FT, 0, s>>>(labels, m, K, hist);
+    ++launches;
+  }
+  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
+                                                                                   p.chunks, acc1, acc2, nanc);
+  big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, out, rows, K, ddof);
+  return launches + 2;
+}
+
+template <int F, typename V, typename L, typename O, int RB>
+int launch_big_sel(const V* values, const L* labels, O* out, long long rows, long long m, long long K,
+                   const FastPlan& p, unsigned char*& cur, cudaStream_t s) {
+  const long long slots = p.blocks * RB * K;
+  unsigned long long* acc = carve<unsigned long long>(cur, slots * 2);
+  // key 0 / index ~0 means "empty" (first: key ~0)
+  if (F == kFirst) cudaMemsetAsync(acc, 0xff, static_cast<size_t>(slots) * 16, s);
+  else if (F == kLast) cudaMemsetAsync(acc, 0, static_cast<size_t>(slots) * 16, s);
+  else init_sel_kernel<<<fin_grid(slots), 256, 0, s>>>(acc, slots);
+  big_sel_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
+                                                                                   p.chunks, acc);
+  big_sel_finish_kernel<F, V, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc, values, out, rows, m, K);
+  return (F == kFirst || F == kLast) ? 2 : 3;
+}
+
 template <int F, typename V, typename L, typename O>
 int launch_fast(const V* values, const L* labels, O* out, long long rows, long long m, long long K, long long ddof,
                 void* ws, size_t ws_bytes, cudaStream_t s) {
@@ -923,7 +1060,9 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   if (!ws || ws_bytes < fast_bytes(F, rows, m, K)) return kWorkspaceTooSmall;
   unsigned char* cur = static_cast<unsigned char*>(ws);
   const long long nctas = rows * p.chunks;
-  if (p.strategy < 2 && nctas > 0x7fffffffll) return kUnsupported;
+  if ((p.strategy < 2 ? nctas : p.blocks * p.chunks) > 0x7fffffffll) return kUnsupported;
+  // the float64 reductions of the large path are not reproducible bit for bit
+  if (p.strategy == 2 && (Need<F>::s1 || Need<F>::s2) && deterministic_mode()) return kUnsupported;
   int launches = 0;
   if (is_moments(F)) {
     if (p.strategy == 0) {
@@ -957,21 +1096,13 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
       launches += 2;
     } else {
-      double* acc1 = carve<double>(cur, rows * K);
-      double* acc2 = carve<double>(cur, Need<F>::s2 ? rows * K : 1);
-      unsigned* nanc = carve<unsigned>(cur, rows * K);
-      unsigned* hist = carve<unsigned>(cur, K);
-      if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(rows * K) * 8, s);
-      if (Need<F>::s2) cudaMemsetAsync(acc2, 0, static_cast<size_t>(rows * K) * 8, s);
-      if (Need<F>::cnt) {
-        cudaMemsetAsync(nanc, 0, static_cast<size_t>(rows * K) * 4, s);
-        cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
-        row_hist_kernel<L><<<fin_grid(m), FT, 0, s>>>(labels, m, K, hist);
-        ++launches;
+      switch (p.rb) {
+        case 16: launches += launch_big_mom<F, V, L, O, 16>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
+        case 8: launches += launch_big_mom<F, V, L, O, 8>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
+        case 4: launches += launch_big_mom<F, V, L, O, 4>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
+        case 2: launches += launch_big_mom<F, V, L, O, 2>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
+        default: launches += launch_big_mom<F, V, L, O, 1>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
       }
-      big_mom_kernel<F, V, L><<<static_cast<int>(nctas), FT, 0, s>>>(values, labels, m, K, p.chunk_len, p.chunks, acc1, acc2, nanc);
-      big_mom_finish_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(acc1, acc2, nanc, hist, out, rows, K, ddof);
-      launches += 2;
     }
   } else {
     if (p.strategy == 0) {
@@ -993,15 +1124,13 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, values, out, rows, m, K, p.chunks, 1);
       launches = 2;
     } else {
-      unsigned long long* acc = carve<unsigned long long>(cur, rows * K * 2);
-      // key 0 / index ~0 means "empty" (first: key ~0)
-      if (F == kFirst) cudaMemsetAsync(acc, 0xff, static_cast<size_t>(rows * K) * 16, s);
-      else if (F == kLast) cudaMemsetAsync(acc, 0, static_cast<size_t>(rows * K) * 16, s);
-      else init_sel_kernel<<<fin_grid(rows * K), 256, 0, s>>>(acc, rows * K);
-      big_sel_kernel<F, V, L><<<static_cast<int>(nctas), FT, 0, s>>>(values, labels, m, K, p.chunk_len, p.chunks, acc);
-      fold_sel_kernel<F, V, O><<<fin_grid(rows * K), 256, 0, s>>>(reinterpret_cast<const SelPart*>(acc), values, out,
-                                                                    rows, m, K, 1, 1);
-      launches = (F == kFirst || F == kLast) ? 2 : 3;
+      switch (p.rb) {
+        case 16: launches = launch_big_sel<F, V, L, O, 16>(values, labels, out, rows, m, K, p, cur, s); break;
+        case 8: launches = launch_big_sel<F, V, L, O, 8>(values, labels, out, rows, m, K, p, cur, s); break;
+        case 4: launches = launch_big_sel<F, V, L, O, 4>(values, labels, out, rows, m, K, p, cur, s); break;
+        case 2: launches = launch_big_sel<F, V, L, O, 2>(values, labels, out, rows, m, K, p, cur, s); break;
+        default: launches = launch_big_sel<F, V, L, O, 1>(values, labels, out, rows, m, K, p, cur, s); break;
+      }
     }
   }
   note_launches(launches);

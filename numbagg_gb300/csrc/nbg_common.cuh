@@ -31,6 +31,8 @@ namespace nbg {
 
 // Host-side count of kernels launched by this library (defined in abi.cu).
 void note_launches(int n);
+// set through nbg_set_deterministic: only run-to-run reproducible algorithms
+bool deterministic_mode();
 
 // ---------------------------------------------------------------------------------
 // error codes shared with the host (include/numbagg_gb300.h)

@@ -119,27 +119,34 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
     out = torch.empty((rows, num_labels), dtype=work, device=flat.device)
     if rows and num_labels:
         L = _lib.lib()
+        # torch.use_deterministic_algorithms(True) selects the reproducible kernels
+        deterministic = torch.are_deterministic_algorithms_enabled()
+        L.nbg_set_deterministic(1 if deterministic else 0)
         fid = _lib.GROUP_FUNC_IDS[name]
         fn = getattr(L, f"nbg_group_{name}_{_host.ALL_SFX[work]}_{'i64' if lab_dt == torch.int64 else 'i32'}")
         for r0 in range(0, rows, _MAX_ROWS):
             r1 = min(rows, r0 + _MAX_ROWS)
             nb = L.nbg_group_workspace_bytes(fid, r1 - r0, m, num_labels)
             ws = _lib.workspaces.scratch(nb, flat.device)
-            _lib.check(
-                fn(
-                    flat[r0:r1].data_ptr() if m else None,
-                    flat_lab.data_ptr() if m else None,
-                    out[r0:r1].data_ptr(),
-                    r1 - r0,
-                    m,
-                    num_labels,
-                    int(ddof),
-                    ws.data_ptr(),
-                    ws.numel(),
-                    _host.stream(flat.device),
-                ),
-                f"group_{name}",
+            status = fn(
+                flat[r0:r1].data_ptr() if m else None,
+                flat_lab.data_ptr() if m else None,
+                out[r0:r1].data_ptr(),
+                r1 - r0,
+                m,
+                num_labels,
+                int(ddof),
+                ws.data_ptr(),
+                ws.numel(),
+                _host.stream(flat.device),
             )
+            if status == _lib.UNSUPPORTED and deterministic:
+                raise RuntimeError(
+                    f"group_{name} with num_labels={num_labels} on floating-point values has no deterministic "
+                    "implementation (its bins do not fit in shared memory), but torch.use_deterministic_algorithms "
+                    "is on"
+                )
+            _lib.check(status, f"group_{name}")
     res = out.reshape(bshape + (num_labels,))
     if work != result_dtype:
         res = res.to(result_dtype)

@@ -373,6 +373,46 @@ def test_prefix_causality_bit_exact(fname):
     assert torch.equal(full[:, :2_000_000][m], part[m])
 
 
+@pytest.fixture
+def deterministic_algorithms():
+    torch.use_deterministic_algorithms(True)
+    try:
+        yield
+    finally:
+        torch.use_deterministic_algorithms(False)
+
+
+@pytest.mark.parametrize("fname", ["group_nansum", "group_nanmean", "group_nanvar", "group_nansum_of_squares"])
+def test_group_deterministic_mode(fname, deterministic_algorithms):
+    # torch.use_deterministic_algorithms(True) routes float moments with a few thousand
+    # labels to the exact fixed-point shared-memory kernels: same bits on every run
+    rng = np.random.default_rng(21)
+    values = rng.standard_normal((6, 300_001))
+    values[rng.random(values.shape) < 0.05] = np.nan
+    values[2, 17] = np.inf
+    labels = rng.integers(-1, 3000, size=300_001)
+    x = torch.from_numpy(values).cuda()
+    lab = torch.from_numpy(labels).cuda()
+    func = getattr(nb, fname)
+    a = func(x, lab, num_labels=3000, axis=-1)
+    b = func(x, lab, num_labels=3000, axis=-1)
+    assert torch.equal(torch.nan_to_num(a, nan=7.0), torch.nan_to_num(b, nan=7.0))
+    want = oracle.group(fname, values, labels, num_labels=3000, axis=-1)
+    scale = np.nanmax(np.abs(np.where(np.isinf(want), np.nan, want)), axis=-1, keepdims=True) * np.ones_like(want)
+    assert_scaled_close(a.cpu().numpy(), want, scale, F64_TOL, None, fname)
+
+
+def test_group_deterministic_mode_refuses_atomic_sums(deterministic_algorithms):
+    x = torch.randn(2, 50_000, dtype=torch.float64, device="cuda")
+    lab = torch.randint(0, 40_000, (50_000,), device="cuda")
+    with pytest.raises(RuntimeError, match="deterministic"):
+        nb.group_nanmean(x, lab, num_labels=40_000, axis=-1)
+    # counts and selections are exact on every path
+    got = nb.group_nancount(x, lab, num_labels=40_000, axis=-1).cpu().numpy()
+    want = oracle.group("group_nancount", x.cpu().numpy(), lab.cpu().numpy(), num_labels=40_000, axis=-1)
+    assert_bit_equal(got, want, "count")
+
+
 def test_determinism_large():
     x = torch.randn(8, 2_000_000, dtype=torch.float64, device="cuda")
     x[torch.rand_like(x) < 0.05] = float("nan")
