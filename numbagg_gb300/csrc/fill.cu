@@ -12,8 +12,10 @@
 // c-th chunk counted from the end of the row.
 //
 // numba types the carried `current` as float64 (unified from `np.nan` and the
-// value), so the stored value is (T)(double)a[j]; for integer dtypes, which have no
-// NaN, that makes the fill an element-wise copy through double.
+// value), so the stored value is (T)(double)a[j].  For float32 and float64 that is
+// a[j] itself, so the float kernel moves bit patterns and never touches a float
+// register; for integer dtypes, which have no NaN, it makes the fill an element-wise
+// copy through double.
 #include "nbg_common.cuh"
 
 #include <mutex>
@@ -22,12 +24,12 @@ namespace nbg {
 namespace fill {
 
 struct Last {
-  long long idx;  // position of the last valid element, -1 if none
-  double val;     // its value as float64 (numba's `current`)
+  long long idx;           // position of the last valid element, -1 if none
+  unsigned long long val;  // its bit pattern (a float32 in the low half)
 };
 
 struct LastOp {
-  NBG_DEVICE Last identity() const { return Last{-1, 0.0}; }
+  NBG_DEVICE Last identity() const { return Last{-1, 0}; }
   NBG_DEVICE Last combine(const Last& earlier, const Last& later) const {
     return later.idx >= 0 ? later : earlier;
   }
@@ -55,17 +57,18 @@ __global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T*
   constexpr long long TILE = WSPAN * (NT / 32);
   constexpr int NW = NT / 32;
   __shared__ long long w_idx[NW];
-  __shared__ double w_val[NW];
+  __shared__ unsigned long long w_val[NW];
   __shared__ int w_first[NW];
   __shared__ long long in_idx[NW];
-  __shared__ double in_val[NW];
+  __shared__ unsigned long long in_val[NW];
   __shared__ long long tile_smem;
   const long long total_tiles = rows * tiles_per_row;
   Workspace ws = make_workspace(ws_base, ws_bytes);
   const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lane_le = 0xffffffffu >> (31 - lane);
-  const T nan = quiet_nan(T(0));
+  typedef typename BitsOf<T>::type B;  // the scan moves bit patterns only
+  const B nan = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
 
   for (;;) {
     if (threadIdx.x == 0) tile_smem = claim_tile(ws.hdr);
@@ -76,29 +79,29 @@ __global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T*
     const long long row = tc.row, chunk = tc.chunk;
     // scan-order position q maps to array position i = q (ffill) or n-1-q (bfill)
     const long long wq0 = chunk * TILE + static_cast<long long>(warp) * WSPAN;
-    const T* ar = a + row * n;
-    T* orow = out + row * n;
+    const B* ar = as_bits(a) + row * n;
+    B* orow = as_bits(out) + row * n;
 
-    T v[K];
+    B v[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       const long long q = wq0 + j * 32 + lane;
-      v[j] = q < n ? __ldcs(ar + (REVERSE ? n - 1 - q : q)) : T(0);
+      v[j] = q < n ? __ldcs(ar + (REVERSE ? n - 1 - q : q)) : B(0);
     }
     long long cidx = -1;  // the warp's running last valid position (uniform)
-    T cval = T(0);
+    B cval = B(0);
     int first = static_cast<int>(WSPAN);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       const long long qb = wq0 + j * 32;
       const long long q = qb + lane;
-      const bool valid = q < n && !is_nan(v[j]);
+      const bool valid = q < n && !nan_bits(v[j]);
       const unsigned msk = __ballot_sync(0xffffffffu, valid);
       const unsigned mle = msk & lane_le;
       const int src = mle ? 31 - __clz(mle) : lane;
-      const T sv = __shfl_sync(0xffffffffu, v[j], src);
+      const B sv = __shfl_sync(0xffffffffu, v[j], src);
       long long ei = cidx;
-      T ev = cval;
+      B ev = cval;
       if (mle) {
         ei = qb + src;
         ev = sv;
@@ -113,13 +116,13 @@ __global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T*
     }
     if (lane == 0) {
       w_idx[warp] = cidx;
-      w_val[warp] = static_cast<double>(cval);
+      w_val[warp] = static_cast<unsigned long long>(cval);
       w_first[warp] = first;
     }
     __syncthreads();
     if (warp == 0) {
       long long li = -1;
-      double lv = 0.0;
+      unsigned long long lv = 0;
       if (lane == 0) {
         for (int w = 0; w < NW; ++w) {  // carry-in of every warp from the earlier warps
           in_idx[w] = li;
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T*
       li = __shfl_sync(0xffffffffu, li, 0);
       lv = __shfl_sync(0xffffffffu, lv, 0);
       const Last agg{li, lv};
-      Last excl{-1, 0.0};
+      Last excl{-1, 0};
       if (chunk == 0) {
         if (lane == 0 && tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
       } else if (agg.idx >= 0) {
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(NT, 3) fill_kernel(const T* __restrict__ a, T*
     // the positions before the warp's first valid element
     if (first > 0) {
       const long long ci = in_idx[warp];
-      const T cv = static_cast<T>(in_val[warp]);
+      const B cv = static_cast<B>(in_val[warp]);
       const long long qend = min(wq0 + first, n);
       for (long long q = wq0 + lane; q < qend; q += 32)
         orow[REVERSE ? n - 1 - q : q] = (ci >= 0 && q - ci <= limit) ? cv : nan;

@@ -144,8 +144,7 @@ struct Dec {
   bool neg;              // sign bit
   bool special;          // infinity or NaN
 };
-NBG_DEVICE Dec decomp(double x) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+NBG_DEVICE Dec decomp(unsigned long long b) {  // float64 bits
   const int eb = static_cast<int>((b >> 52) & 0x7ff);
   Dec d;
   d.m = (b & 0x000fffffffffffffull) | (eb ? 0x0010000000000000ull : 0ull);
@@ -154,9 +153,8 @@ NBG_DEVICE Dec decomp(double x) {
   d.special = eb == 0x7ff;
   return d;
 }
-// a float32 restated exactly in the float64 format
-NBG_DEVICE Dec decomp(float x) {
-  const unsigned b = static_cast<unsigned>(__float_as_int(x));
+// float32 bits, restated exactly in the float64 format
+NBG_DEVICE Dec decomp(unsigned b) {
   const int eb = static_cast<int>((b >> 23) & 0xff);
   Dec d;
   d.m = static_cast<unsigned long long>((b & 0x7fffffu) | (eb ? 0x800000u : 0u)) << 29;
@@ -167,15 +165,27 @@ NBG_DEVICE Dec decomp(float x) {
 }
 // integer values reach the moment kernels only through the generic path; these keep
 // the templates well-formed
-NBG_DEVICE Dec decomp(int x) { return decomp(static_cast<double>(x)); }
-NBG_DEVICE Dec decomp(long long x) { return decomp(static_cast<double>(x)); }
+NBG_DEVICE Dec decomp(int x) {
+  return decomp(static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
+}
+NBG_DEVICE Dec decomp(long long x) {
+  return decomp(static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
+}
 
-// Order key of a value for the selection functions: a < b (compared as float64, the
-// reference's comparison) <=> key(a) < key(b), -0.0 and +0.0 equal, and no key is 0
-// (0 marks an empty bin).
-NBG_DEVICE unsigned long long value_key(double v) { return order_key_ieee(v); }
-NBG_DEVICE unsigned long long value_key(float v) {
-  unsigned b = static_cast<unsigned>(__float_as_int(v));
+// the value of a bit pattern as float64
+NBG_DEVICE double bits_to_f64(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
+NBG_DEVICE double bits_to_f64(unsigned b) { return static_cast<double>(__int_as_float(static_cast<int>(b))); }
+NBG_DEVICE double bits_to_f64(int v) { return static_cast<double>(v); }
+NBG_DEVICE double bits_to_f64(long long v) { return static_cast<double>(v); }
+
+// Order key of a value (given as its bits, see BitsOf) for the selection functions:
+// a < b (compared as float64, the reference's comparison) <=> key(a) < key(b), -0.0
+// and +0.0 equal, and no key is 0 (0 marks an empty bin).
+NBG_DEVICE unsigned long long value_key(unsigned long long b) {  // float64 bits
+  if ((b << 1) == 0) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+NBG_DEVICE unsigned long long value_key(unsigned b) {  // float32 bits
   if ((b << 1) == 0) b = 0;
   return (b >> 31) ? static_cast<unsigned long long>(~b) : static_cast<unsigned long long>(b | 0x80000000u);
 }
@@ -207,6 +217,7 @@ __global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ v
                                                          long long rows, long long m, int K, long long chunk_len,
                                                          long long chunks, int d1, int d2,
                                                          MomPart* __restrict__ parts) {
+  typedef typename BitsOf<V>::type B;
   constexpr bool S1 = Need<F>::s1, S2 = Need<F>::s2, CNT = Need<F>::cnt, VL = Need<F>::varlike;
   constexpr bool MOM = S1 || S2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -228,24 +239,24 @@ __global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ v
   }
   if (tid < 2 * kTinyK) infs[tid / kTinyK][tid % kTinyK] = 0;
   __syncthreads();
-  const V* vr = values + row * m;
+  const B* vr = as_bits(values) + row * m;
   int E = 0;  // the warp's scale (uniform across the warp)
   for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
        base += static_cast<long long>(FT / 32) * kTileCols) {
-    V v[16];
+    B v[16];
     int lab[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const long long col = base + j * 32 + lane;
       const bool in = col < c1;
-      v[j] = in ? __ldcs(vr + col) : V(0);
+      v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
       lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
     }
     int emax = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      if (is_nan(v[j])) lab[j] = -1;
+      if (nan_bits(v[j])) lab[j] = -1;
       if (MOM) {
         const Dec d = decomp(v[j]);
         if (lab[j] >= 0 && !d.special && !(VL && d.e >= 1023 + 512)) emax = max(emax, d.e);
@@ -349,6 +360,7 @@ template <int F, typename V, typename L>
 __global__ void __launch_bounds__(FT, 2) tiny_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                          long long rows, long long m, int K, long long chunk_len,
                                                          long long chunks, SelPart* __restrict__ parts) {
+  typedef typename BitsOf<V>::type B;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* bk = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][FT]
   unsigned long long* bi = bk + K * FT;                                     // [K][FT]
@@ -362,18 +374,18 @@ __global__ void __launch_bounds__(FT, 2) tiny_sel_kernel(const V* __restrict__ v
     bk[k * FT + tid] = (F == kFirst) ? ~0ull : 0ull;
     bi[k * FT + tid] = ~0ull;
   }
-  const V* vr = values + row * m;
+  const B* vr = as_bits(values) + row * m;
   for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
        base += static_cast<long long>(FT / 32) * kTileCols) {
-    V v[16];
+    B v[16];
     int lab[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const long long col = base + j * 32 + lane;
       const bool in = col < c1;
-      v[j] = in ? __ldcs(vr + col) : V(0);
+      v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
-      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
+      lab[j] = (l >= 0 && l < K && !nan_bits(v[j])) ? static_cast<int>(l) : -1;
     }
     // a lane meets its columns in increasing order
 #pragma unroll
@@ -476,6 +488,7 @@ __global__ void __launch_bounds__(FT) mid_mom_kernel(const V* __restrict__ value
                                                      long long rows, long long m, int K, long long chunk_len,
                                                      long long chunks, const unsigned* __restrict__ hist,
                                                      MomPart* __restrict__ parts) {
+  typedef typename BitsOf<V>::type B;
   constexpr bool S1 = Need<F>::s1, S2 = Need<F>::s2, CNT = Need<F>::cnt, VL = Need<F>::varlike;
   constexpr bool MOM = S1 || S2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -512,25 +525,25 @@ __global__ void __launch_bounds__(FT) mid_mom_kernel(const V* __restrict__ value
   __syncthreads();
   // also bounds the infinities per counter (2^15 of each fit in the packed word)
   const long long flush_len = (hmax <= kMaxTermsPerFlush) ? chunk_len : kMaxTermsPerFlush;
-  const V* vr = values + row * m;
+  const B* vr = as_bits(values) + row * m;
   int E = 0;  // the CTA's scale, the same in every thread
   for (long long sub = c0; sub < c1; sub += flush_len) {
     const long long send = min(c1, sub + flush_len);
     for (long long base = sub; base < send; base += kCtaCols) {
-      V v[8];
+      B v[8];
       int lab[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const long long col = base + j * FT + tid;
         const bool in = col < send;
-        v[j] = in ? __ldcs(vr + col) : V(0);
+        v[j] = in ? __ldcs(vr + col) : B(0);
         const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
         lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
       }
       int emax = 0;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        if (lab[j] >= 0 && is_nan(v[j])) {
+        if (lab[j] >= 0 && nan_bits(v[j])) {
           if (CNT) atomicAdd(&nanc[lab[j]], 1u);
           lab[j] = -1;
         }
@@ -613,6 +626,7 @@ template <int F, typename V, typename L>
 __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                      long long rows, long long m, int K, long long chunk_len,
                                                      long long chunks, SelPart* __restrict__ parts) {
+  typedef typename BitsOf<V>::type B;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* bins = reinterpret_cast<unsigned long long*>(smem_raw);  // [K][2]
   const int tid = threadIdx.x;
@@ -624,18 +638,21 @@ __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ value
     bins[2 * k + 1] = ~0ull;
   }
   __syncthreads();
-  const V* vr = values + row * m;
+  const B* vr = as_bits(values) + row * m;
   for (long long base = c0; base < c1; base += kCtaCols) {
-    V v[8];
+    B v[8];
     int lab[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const long long col = base + j * FT + tid;
       const bool in = col < c1;
-      v[j] = in ? __ldcs(vr + col) : V(0);
+      v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
-      lab[j] = (l >= 0 && l < K && !is_nan(v[j])) ? static_cast<int>(l) : -1;
+      lab[j] = (l >= 0 && l < K && !nan_bits(v[j])) ? static_cast<int>(l) : -1;
     }
+    // Every lane runs the whole update (its loads, then a compare-and-swap loop that
+    // rarely iterates): measured several times faster here than first filtering on
+    // the bin's key, which makes the warp diverge around the loop.
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       if (lab[j] < 0) continue;
@@ -679,32 +696,41 @@ struct BigStage {  // per warp: U sub-tiles of RB rows x 32 columns, rows padded
   V s[FT / 32][U][RB][P];
 };
 
-// Loads RB rows x 32U columns of the row block (lanes along the columns) and calls
-// f(u, v, l, live) for lane (r = lane % RB, g = lane / RB) on the RB elements it
-// reduces of each sub-tile u: value v of row r, label l of its column (-1 past c1).
+// Loads RB rows x 32U columns of the row block (lanes along the columns) and hands
+// f the kBigT elements that lane (r = lane % RB, g = lane / RB) reduces: value of row
+// r and label of its column (-1 past c1; labels are below 2^31), with the tile's first
+// column (big_col gives each element's column).
 template <typename V, typename L, int RB, typename Fn>
 NBG_DEVICE void big_tiles(const V* __restrict__ values, const L* __restrict__ labels, long long rows, long long m,
-                          long long rb, long long c0, long long c1, BigStage<V, RB>& st, Fn&& f) {
-  constexpr int U = BigStage<V, RB>::U, G = 32 / RB;
+                          long long rb, long long c0, long long c1, BigStage<typename BitsOf<V>::type, RB>& st,
+                          Fn&& f) {
+  typedef typename BitsOf<V>::type B;
+  constexpr int U = BigStage<B, RB>::U, G = 32 / RB;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int r = lane % RB, g = lane / RB;
   const long long row0 = rb * RB;
+  const unsigned long long stream = l2_evict_first();
   for (long long cbase = c0 + static_cast<long long>(warp) * 32 * U; cbase < c1;
        cbase += static_cast<long long>(FT / 32) * 32 * U) {
-    V x[U][RB];
+    B x[U][RB];
     long long lab[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const long long col = cbase + u * 32 + lane;
       const bool in = col < c1;
-      lab[u] = in ? static_cast<long long>(__ldg(labels + col)) : -1;
+      lab[u] = in ? static_cast<long long>(ld_hint(labels + col, stream)) : -1;
 #pragma unroll
       for (int rr = 0; rr < RB; ++rr)
-        x[u][rr] = (in && row0 + rr < rows) ? __ldcs(values + (row0 + rr) * m + col) : V(0);
+        x[u][rr] = (in && row0 + rr < rows) ? ld_hint(as_bits(values) + (row0 + rr) * m + col, stream) : B(0);
     }
+    B ev[kBigT];
+    int el[kBigT];
     if (RB == 1) {
 #pragma unroll
-      for (int u = 0; u < U; ++u) f(u, x[u][0], lab[u], cbase + u * 32 + lane);
+      for (int u = 0; u < U; ++u) {
+        ev[u] = x[u][0];
+        el[u] = static_cast<int>(lab[u]);
+      }
     } else {
 #pragma unroll
       for (int u = 0; u < U; ++u)
@@ -716,69 +742,107 @@ NBG_DEVICE void big_tiles(const V* __restrict__ values, const L* __restrict__ la
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
           const int c = i * G + g;
-          const long long l = __shfl_sync(0xffffffffu, lab[u], c);
-          f(u, st.s[warp][u][r][c], l, cbase + u * 32 + c);
+          ev[u * RB + i] = st.s[warp][u][r][c];
+          el[u * RB + i] = static_cast<int>(__shfl_sync(0xffffffffu, lab[u], c));
         }
       }
       __syncwarp();
     }
+    f(ev, el, cbase);
   }
 }
 
+// column of element e of big_tiles' lane arrays, in the tile starting at cbase
+template <int RB>
+NBG_DEVICE long long big_col(long long cbase, int e) {
+  const int lane = threadIdx.x & 31;
+  if (RB == 1) return cbase + e * 32 + lane;
+  return cbase + (e / RB) * 32 + (e % RB) * (32 / RB) + lane / RB;
+}
+
 template <int F, typename V, typename L, int RB>
-__global__ void __launch_bounds__(FT) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+__global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                      long long rows, long long m, long long K, long long chunk_len,
                                                      long long chunks, double* __restrict__ acc1,
                                                      double* __restrict__ acc2, unsigned* __restrict__ nanc) {
-  __shared__ BigStage<V, RB> st;
+  typedef typename BitsOf<V>::type B;
+  __shared__ BigStage<B, RB> st;
   const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
   const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
   const int r = (threadIdx.x & 31) % RB;
   const bool live = rb * RB + r < rows;
   const long long off = rb * K * RB + r;  // accumulator of (label l, row r): off + l * RB
-  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st, [&](int, V v, long long l, long long) {
-    if (!live || l < 0 || l >= K) return;
-    const long long a = off + l * RB;
-    if (is_nan(v)) {
-      if (Need<F>::cnt) atomicAdd(&nanc[a], 1u);
-      return;
-    }
-    const double x = static_cast<double>(v);
-    if (Need<F>::s1) atomicAdd(&acc1[a], x);
-    if (Need<F>::s2) atomicAdd(&acc2[a], x * x);
-  });
+  const unsigned long long keep = l2_evict_last();
+  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st,
+                      [&](const B (&ev)[kBigT], const int (&el)[kBigT], long long) {
+#pragma unroll
+                        for (int e = 0; e < kBigT; ++e) {
+                          const long long l = el[e];
+                          if (!live || l < 0 || l >= K) continue;
+                          const long long a = off + l * RB;
+                          if (nan_bits(ev[e])) {
+                            if (Need<F>::cnt) red_add_hint(&nanc[a], 1u, keep);
+                            continue;
+                          }
+                          const double x = bits_to_f64(ev[e]);
+                          if (Need<F>::s1) red_add_hint(&acc1[a], x, keep);
+                          if (Need<F>::s2) red_add_hint(&acc2[a], x * x, keep);
+                        }
+                      });
 }
 
-__global__ void init_sel_kernel(unsigned long long* __restrict__ acc, long long n) {
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
-    acc[2 * t] = 0ull;       // key 0 is below every real key
-    acc[2 * t + 1] = ~0ull;  // no index yet
-  }
-}
 
-template <int F, typename V, typename L, int RB>
-__global__ void __launch_bounds__(FT) big_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
-                                                     long long rows, long long m, long long K, long long chunk_len,
-                                                     long long chunks, unsigned long long* __restrict__ acc) {
-  __shared__ BigStage<V, RB> st;
+// Selection with many labels, in two passes of fire-and-forget L2 reductions (no
+// compare-and-swap round trips): pass 0 reduces every bin's order key with max
+// (first / last: the column with min / max, which finishes the job); pass 1 reads the
+// data again and reduces the column with min wherever an element's key equals its
+// bin's maximum -- the first column holding the maximum, as the reference's strict
+// comparison keeps.  Exact and independent of the order of the reductions.
+template <int F, typename V, typename L, int RB, int PASS>
+__global__ void __launch_bounds__(FT, 2) big_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                        long long rows, long long m, long long K, long long chunk_len,
+                                                        long long chunks, unsigned long long* __restrict__ kmax,
+                                                        unsigned long long* __restrict__ imin) {
+  typedef typename BitsOf<V>::type B;
+  __shared__ BigStage<B, RB> st;
   const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
   const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
   const int r = (threadIdx.x & 31) % RB;
   const bool live = rb * RB + r < rows;
   const long long off = rb * K * RB + r;
-  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st, [&](int, V v, long long l, long long col) {
-    if (!live || l < 0 || l >= K || is_nan(v)) return;
-    const unsigned long long c = static_cast<unsigned long long>(col);
-    unsigned long long* p = acc + 2 * (off + l * RB);
-    if (F == kFirst) {
-      if (c < __ldcg(p)) atomicMin(p, c);
-    } else if (F == kLast) {
-      atomicMax(p, c + 1);
-    } else {
-      sel_update(p, sel_key_of<F>(v), c, false);
-    }
-  });
+  const unsigned long long keep = l2_evict_last();
+  big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st,
+                      [&](const B (&ev)[kBigT], const int (&el)[kBigT], long long cbase) {
+                        if (PASS == 0) {
+#pragma unroll
+                          for (int e = 0; e < kBigT; ++e) {
+                            const int l = el[e];
+                            if (!live || l < 0 || l >= K || nan_bits(ev[e])) continue;
+                            const long long a = off + static_cast<long long>(l) * RB;
+                            const unsigned long long c = static_cast<unsigned long long>(big_col<RB>(cbase, e));
+                            if (F == kFirst) red_min_hint(&imin[a], c, keep);
+                            else if (F == kLast) red_max_hint(&kmax[a], c + 1, keep);
+                            else red_max_hint(&kmax[a], sel_key_of<F>(ev[e]), keep);
+                          }
+                        } else {
+                          unsigned long long best[kBigT];  // independent loads, all in flight
+#pragma unroll
+                          for (int e = 0; e < kBigT; ++e) {
+                            const int l = el[e];
+                            best[e] = 0;
+                            if (live && l >= 0 && l < K)
+                              best[e] = ld_keep(&kmax[off + static_cast<long long>(l) * RB], keep);
+                          }
+#pragma unroll
+                          for (int e = 0; e < kBigT; ++e) {
+                            const int l = el[e];
+                            if (!live || l < 0 || l >= K || nan_bits(ev[e])) continue;
+                            if (sel_key_of<F>(ev[e]) != best[e]) continue;
+                            red_min_hint(&imin[off + static_cast<long long>(l) * RB],
+                                         static_cast<unsigned long long>(big_col<RB>(cbase, e)), keep);
+                          }
+                        }
+                      });
 }
 
 // ---------------------------------------------------------------------------------
@@ -869,7 +933,8 @@ NBG_DEVICE O finish_sel(unsigned long long key, unsigned long long idx, const V*
 }
 
 template <int F, typename V, typename O, int RB>
-__global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ acc, const V* __restrict__ values,
+__global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ kmax,
+                                      const unsigned long long* __restrict__ imin, const V* __restrict__ values,
                                       O* __restrict__ out, long long rows, long long m, long long K) {
   const long long total = (rows + RB - 1) / RB * K * RB;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
@@ -877,7 +942,10 @@ __global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ acc
     const long long rb = t / (K * RB), rem = t - rb * K * RB;
     const long long k = rem / RB, row = rb * RB + (rem - k * RB);
     if (row >= rows) continue;
-    out[row * K + k] = finish_sel<F, V, O>(acc[2 * t], acc[2 * t + 1], values + row * m);
+    // finish_sel's (key, index) convention: first keeps its column in the key
+    const unsigned long long key = F == kFirst ? imin[t] : kmax[t];
+    const unsigned long long idx = (F == kFirst || F == kLast) ? 0ull : (kmax[t] ? imin[t] : ~0ull);
+    out[row * K + k] = finish_sel<F, V, O>(key, idx, values + row * m);
   }
 }
 
@@ -924,7 +992,8 @@ inline int big_rows_per_block(int f, long long rows, long long K) {
     if (f == kVar || f == kStd || f == kSumSq) per += 8;
   }
   int rb = 16;
-  while (rb > 1 && (rb / 2 >= rows || static_cast<size_t>(K) * rb * per > (64ull << 20))) rb /= 2;
+  const size_t budget = 64ull << 20;
+  while (rb > 1 && (rb / 2 >= rows || static_cast<size_t>(K) * rb * per > budget)) rb /= 2;
   return rb;
 }
 
@@ -1042,15 +1111,19 @@ template <int F, typename V, typename L, typename O, int RB>
 int launch_big_sel(const V* values, const L* labels, O* out, long long rows, long long m, long long K,
                    const FastPlan& p, unsigned char*& cur, cudaStream_t s) {
   const long long slots = p.blocks * RB * K;
-  unsigned long long* acc = carve<unsigned long long>(cur, slots * 2);
-  // key 0 / index ~0 means "empty" (first: key ~0)
-  if (F == kFirst) cudaMemsetAsync(acc, 0xff, static_cast<size_t>(slots) * 16, s);
-  else if (F == kLast) cudaMemsetAsync(acc, 0, static_cast<size_t>(slots) * 16, s);
-  else init_sel_kernel<<<fin_grid(slots), 256, 0, s>>>(acc, slots);
-  big_sel_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
-                                                                                   p.chunks, acc);
-  big_sel_finish_kernel<F, V, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc, values, out, rows, m, K);
-  return (F == kFirst || F == kLast) ? 2 : 3;
+  unsigned long long* kmax = carve<unsigned long long>(cur, slots);
+  unsigned long long* imin = carve<unsigned long long>(cur, slots);
+  cudaMemsetAsync(kmax, 0, static_cast<size_t>(slots) * 8, s);     // below every key and column + 1
+  cudaMemsetAsync(imin, 0xff, static_cast<size_t>(slots) * 8, s);  // no column yet
+  const int grid = static_cast<int>(p.blocks * p.chunks);
+  big_sel_kernel<F, V, L, RB, 0><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax, imin);
+  int launches = 1;
+  if (F != kFirst && F != kLast) {
+    big_sel_kernel<F, V, L, RB, 1><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax, imin);
+    ++launches;
+  }
+  big_sel_finish_kernel<F, V, O, RB><<<fin_grid(slots), 256, 0, s>>>(kmax, imin, values, out, rows, m, K);
+  return launches + 1;
 }
 
 template <int F, typename V, typename L, typename O>

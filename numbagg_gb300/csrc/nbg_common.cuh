@@ -50,6 +50,97 @@ enum Status : int {
 // ---------------------------------------------------------------------------------
 // bit-level predicates
 // ---------------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------
+// L2 cache policies: inputs streamed once are read with evict-first so that they do
+// not displace data that is reused (reduction targets, shared labels), which is
+// updated with evict-last.
+// ---------------------------------------------------------------------------------
+NBG_DEVICE unsigned long long l2_evict_first() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+NBG_DEVICE unsigned long long l2_evict_last() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+NBG_DEVICE double ld_hint(const double* a, unsigned long long pol) {
+  double v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE float ld_hint(const float* a, unsigned long long pol) {
+  float v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE int ld_hint(const int* a, unsigned long long pol) {
+  int v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE long long ld_hint(const long long* a, unsigned long long pol) {
+  long long v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE void red_add_hint(double* a, double v, unsigned long long pol) {
+  asm volatile("red.global.add.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(a), "d"(v), "l"(pol) : "memory");
+}
+NBG_DEVICE void red_max_hint(unsigned long long* a, unsigned long long v, unsigned long long pol) {
+  asm volatile("red.global.max.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(a), "l"(v), "l"(pol) : "memory");
+}
+NBG_DEVICE void red_min_hint(unsigned long long* a, unsigned long long v, unsigned long long pol) {
+  asm volatile("red.global.min.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(a), "l"(v), "l"(pol) : "memory");
+}
+NBG_DEVICE unsigned long long ld_keep(const unsigned long long* a, unsigned long long pol) {
+  unsigned long long v;
+  asm volatile("ld.global.cg.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE void red_add_hint(unsigned* a, unsigned v, unsigned long long pol) {
+  asm volatile("red.global.add.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+}
+
+// Values handled as raw bits.  Loading a float array through its integer twin keeps
+// every test on the integer pipes: a NaN test on a float64 register can be compiled
+// to a float64 compare, and this GPU's FP64 pipe takes 16 cycles per warp instruction.
+template <typename T>
+struct BitsOf {
+  typedef T type;  // integers are their own bits
+};
+template <>
+struct BitsOf<double> {
+  typedef unsigned long long type;
+};
+template <>
+struct BitsOf<float> {
+  typedef unsigned type;
+};
+NBG_DEVICE bool nan_bits(unsigned long long b) { return (b << 1) > 0xffe0000000000000ull; }
+NBG_DEVICE bool nan_bits(unsigned b) { return (b << 1) > 0xff000000u; }
+NBG_DEVICE bool nan_bits(int) { return false; }
+NBG_DEVICE bool nan_bits(long long) { return false; }
+template <typename T>
+NBG_DEVICE const typename BitsOf<T>::type* as_bits(const T* p) {
+  return reinterpret_cast<const typename BitsOf<T>::type*>(p);
+}
+template <typename T>
+NBG_DEVICE typename BitsOf<T>::type* as_bits(T* p) {
+  return reinterpret_cast<typename BitsOf<T>::type*>(p);
+}
+NBG_DEVICE unsigned long long ld_hint(const unsigned long long* a, unsigned long long pol) {
+  unsigned long long v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(pol));
+  return v;
+}
+NBG_DEVICE unsigned ld_hint(const unsigned* a, unsigned long long pol) {
+  unsigned v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
 // the quiet NaN numpy writes (np.nan), in the type of the argument
 NBG_DEVICE double quiet_nan(double) { return __longlong_as_double(0x7ff8000000000000ll); }
 NBG_DEVICE float quiet_nan(float) { return __int_as_float(0x7fc00000); }
