@@ -59,6 +59,12 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cols", type=int, default=COLS, help="columns (smaller for quick runs)")
     p.add_argument("--only", default=None, help="regex: time only the calls whose key matches (profiling)")
+    p.add_argument(
+        "--suite",
+        choices=("group_fill", "scan"),
+        default="group_fill",
+        help="group_fill: the headline workload; scan: the moving-window, EWM and matrix shapes",
+    )
     return p.parse_args(argv)
 
 
@@ -513,10 +519,152 @@ def run_e2e(args, nb, values, labels, fill, calls, device, world):
     }
 
 
+# ---- the scan suite: moving windows, EWM, matrices -----------------------------------------
+
+SCAN_ROWS, SCAN_COLS = 1024, 1_048_576  # precision-stress shape
+SCAN_WINDOWS = (5, 252, 10_000)
+SCAN_ALPHAS = (0.5, 0.01, 1e-4)
+SMALL_ROWS, SMALL_COLS = 100, 10_000  # the reference's CPU-runnable move_mean case
+MATRIX_T, MATRIX_V = 65_536, 256
+
+
+def scan_inputs(device, cols):
+    """a = 1e6 + z1, b = 1e6 + 0.7 z1 + sqrt(0.51) z2 (correlation 0.7), 2% NaN each."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(3)
+    z1 = torch.randn((SCAN_ROWS, cols), generator=g, dtype=torch.float64, device=device)
+    b = torch.randn((SCAN_ROWS, cols), generator=g, dtype=torch.float64, device=device)
+    b.mul_(math.sqrt(0.51)).add_(z1, alpha=0.7).add_(1e6)
+    a = z1.add_(1e6)
+    a[torch.rand(a.shape, generator=g, device=device) < 0.02] = float("nan")
+    b[torch.rand(b.shape, generator=g, device=device) < 0.02] = float("nan")
+    g.manual_seed(0)
+    small = torch.randn((SMALL_ROWS, SMALL_COLS), generator=g, dtype=torch.float64, device=device)
+    small[torch.rand(small.shape, generator=g, device=device) < 0.10] = float("nan")
+    g.manual_seed(4)
+    A = torch.randn((MATRIX_V, MATRIX_V), generator=g, dtype=torch.float64, device=device) / 16.0
+    Z = torch.randn((MATRIX_T, MATRIX_V), generator=g, dtype=torch.float64, device=device)
+    X = (Z @ A.T).to(torch.float32)
+    X[torch.rand(X.shape, generator=g, device=device) < 0.01] = float("nan")
+    return a, b, small, X
+
+
+def scan_calls(cols):
+    """(key, callable(nb, a, b, small, X), algorithmic bytes, elements) of the scan suite.
+    min_count = window // 2: with 2% NaN the default (= window) leaves almost every
+    output NaN at the two larger windows."""
+    R, N = SCAN_ROWS, cols
+    out = []
+    for w in SCAN_WINDOWS:
+        out.append((f"move_std_w{w}", lambda nb, a, b, s, X, w=w: nb.move_std(a, window=w, min_count=w // 2), 16 * R * N, R * N))
+    for w in SCAN_WINDOWS:
+        out.append(
+            (f"move_corr_w{w}", lambda nb, a, b, s, X, w=w: nb.move_corr(a, b, window=w, min_count=w // 2), 24 * R * N, R * N)
+        )
+    for al in SCAN_ALPHAS:
+        out.append((f"move_exp_nanmean_a{al:g}", lambda nb, a, b, s, X, al=al: nb.move_exp_nanmean(a, alpha=al), 16 * R * N, R * N))
+        out.append((f"move_exp_nanvar_a{al:g}", lambda nb, a, b, s, X, al=al: nb.move_exp_nanvar(a, alpha=al), 16 * R * N, R * N))
+        out.append(
+            (f"move_exp_nancorr_a{al:g}", lambda nb, a, b, s, X, al=al: nb.move_exp_nancorr(a, b, alpha=al), 24 * R * N, R * N)
+        )
+    T, V = MATRIX_T, MATRIX_V
+    for f in ("move_covmatrix", "move_corrmatrix"):
+        out.append((f"{f}_w500", lambda nb, a, b, s, X, f=f: getattr(nb, f)(X, window=500, min_count=400), 4 * T * V + 4 * T * V * V, T * V))
+    return out
+
+
+def run_scan_suite(args):
+    import re
+
+    import torch
+
+    import numbagg_gb300 as nb
+    from numbagg_gb300 import _lib
+
+    world, rank, local = dist_env()
+    device = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+    cols = min(args.cols, SCAN_COLS)
+    a, b, small, X = scan_inputs(device, cols)
+    calls = scan_calls(cols)
+    if args.only:
+        calls = [c for c in calls if re.search(args.only, c[0])]
+    peak, peak_kind = measured_peak()
+    stream = torch.cuda.current_stream(device)
+    per_func = {}
+    launches0 = _lib.launch_count()
+    for key, fn, nbytes, elems in calls:
+        for _ in range(args.warmup):
+            fn(nb, a, b, small, X)
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn(nb, a, b, small, X)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = nbytes / (ms / 1000.0) / 1e9
+        per_func[key] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4), "Gelem/s": round(elems / ms / 1e6, 2)}
+    # the 100 x 10,000 move_mean (16 MB, resident in L2): replayed from a CUDA graph
+    if not args.only or re.search(args.only, "move_mean_small"):
+        fn = lambda: nb.move_mean(small, window=20, min_count=20)  # noqa: E731
+        s2 = torch.cuda.Stream(device)
+        s2.wait_stream(stream)
+        with torch.cuda.stream(s2):
+            for _ in range(3):
+                fn()
+        stream.wait_stream(s2)
+        torch.cuda.synchronize(device)
+        graph = torch.cuda.CUDAGraph()
+        reps = 100
+        with torch.cuda.graph(graph, stream=s2):
+            for _ in range(reps):
+                fn()
+        graph.replay()
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(10):
+            graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        us = e0.elapsed_time(e1) * 1000.0 / (10 * reps)
+        nbytes = 16 * SMALL_ROWS * SMALL_COLS
+        per_func["move_mean_small_w20"] = {
+            "us": round(us, 2),
+            "GB/s": round(nbytes / (us / 1e6) / 1e9, 1),
+            "note": "16 MB, L2-resident; 1000 launches replayed from CUDA graphs",
+        }
+    line = {
+        "suite": "scan",
+        "unit": "GB/s",
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "dtype": "f64 (matrices: f32 in, f32 out)",
+        "config": {
+            "scan": f"{SCAN_ROWS}x{cols} float64, a = 1e6 + z1, b = 1e6 + 0.7 z1 + sqrt(0.51) z2, 2% NaN; min_count = window // 2",
+            "matrix": f"{MATRIX_T}x{MATRIX_V} float32 from N(0, A A^T / 256), 1% NaN, window 500, min_count 400",
+            "small": f"{SMALL_ROWS}x{SMALL_COLS} float64 N(0,1), 10% NaN, window 20, min_count 20",
+        },
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "gpu_launches": int(_lib.launch_count() - launches0),
+        "per_func": per_func,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
+    if args.suite == "scan":
+        return run_scan_suite(args)
     return run_ours(args)
 
 

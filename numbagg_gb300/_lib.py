@@ -158,7 +158,8 @@ class _Workspaces:
                 size = max(nbytes, 1 << 20)
                 if buf is not None:
                     size = max(size, 2 * buf.numel())
-                torch.cuda.current_stream(device).synchronize()
+                # the old buffer was used on this stream only, so the caching allocator
+                # orders its reuse; no synchronisation (which stream capture forbids)
                 buf = torch.zeros(size, dtype=torch.uint8, device=device)
                 self._scan[key] = buf
             return buf
