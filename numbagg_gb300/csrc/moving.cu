@@ -12,23 +12,39 @@
 // (fixed128.cuh) at the scale of the largest exponent in the tile, so every window
 // sum is exact (to 2^-80 of its largest term) whatever the position in the row: the
 // reference's own add/subtract drift is the only difference left between the two.
-// Integer addition is associative, so results are bit-identical for any tiling and
-// run to run.  The exact sums are rounded once to float64 and finalised with the
-// reference's formulas; divisions by the count use a per-CTA table of correctly
-// rounded reciprocals and Markstein's correction (q0 = s*r; e = fma(-q0, c, s);
-// q = fma(e, r, q0); P. Markstein, IBM J. Res. Dev. 34(1), 1990), which returns s / c.
+// Integer addition is associative, so results do not depend on how a row is cut into
+// chunks and tiles, and are the same run to run, as long as no valid value in a row is
+// more than 2^40 times smaller than the largest one met before it in its chunk (those
+// would lose bits below the fixed-point LSB).  The exact sums are rounded once to
+// float64 with integer instructions only and finalised with the reference's formulas.
+// The division of the mean and of the squared sum by the count is correctly rounded
+// (a table of reciprocals 1/c and Markstein's correction: q0 = s*r; e = fma(-q0, c, s);
+// q = fma(e, r, q0); P. Markstein, IBM J. Res. Dev. 34(1), 1990), so exact zero
+// variances stay zero; the final division by count - 1 multiplies by 1/(c - 1)
+// (within one ulp of the quotient).  This GPU's FP64 pipe takes 16 cycles per warp
+// instruction, so the finalisation is what bounds these kernels.
 //
 // Infinities follow the reference: an infinity in the running sum makes every later
 // sum NaN once it leaves the window (inf - inf), or while infinities of both signs
 // are inside; for the variance-like statistics any infinity (or |x| >= 2^512, whose
 // square overflows) turns the rest of the row NaN.  These are tracked as counts.
 //
-// Parallel structure: a row is cut into tiles of NT*K positions; each thread scans K
-// consecutive positions serially, warp shuffles combine threads, and the state
-// entering a tile comes from a decoupled look-back whose combine step aligns the two
-// tiles' scales.  Accumulation is exact for float32 arrays too (numba keeps float64
-// accumulators there, numbagg/moving.py:16); the result is rounded to float32.
+// Parallel structure: a row is cut into chunks of at least 8 windows; a CTA seeds its
+// chunk with the exact sums of the window before it (the w values preceding the chunk)
+// and walks the chunk in sub-tiles of 2048 positions: coalesced loads of the entering
+// and leaving values through a padded shared stage, 8 consecutive positions per
+// thread, a block scan of the thread totals and a carry into the next sub-tile.  The
+// scale only grows along the chunk (the carry is shifted when it does).  No state
+// crosses chunks, except that the reference never recovers from an infinity: once one
+// has left the window (sum, mean) or entered it (variance-like statistics) every later
+// output of the row is NaN; the kernels record each row's first such position and a
+// second kernel writes the NaNs after it.  Accumulation is exact for float32 arrays
+// too (numba keeps float64 accumulators there, numbagg/moving.py:16); the result is
+// rounded to float32.
 #include "fixed128.cuh"
+
+#include <algorithm>
+#include <climits>
 
 namespace nbg {
 namespace moving {
@@ -74,12 +90,6 @@ struct Sums {  // tile-local moments (one scale for the whole tile)
   int pad;
 };
 
-template <int NS>
-struct XState {  // a state that travels between tiles: sums plus their scale
-  Sums<NS> m;
-  int ea, eb;
-  int pad0, pad1;
-};
 
 template <int NS>
 NBG_DEVICE Sums<NS> zero_sums() {
@@ -116,66 +126,101 @@ NBG_DEVICE Sums<Traits<OP>::NS> rescale(const Sums<Traits<OP>::NS>& v, int ea, i
   return r;
 }
 
-template <int OP>
-struct CombineOp {
-  using X = XState<Traits<OP>::NS>;
-  NBG_DEVICE X identity() const {
-    X x;
-    x.m = zero_sums<Traits<OP>::NS>();
-    x.ea = x.eb = 0;
-    x.pad0 = x.pad1 = 0;
-    return x;
-  }
-  NBG_DEVICE X combine(const X& e, const X& l) const {
-    X r;
-    r.ea = max(e.ea, l.ea);
-    r.eb = max(e.eb, l.eb);
-    r.m = add(rescale<OP>(e.m, e.ea, e.eb, r.ea, r.eb), rescale<OP>(l.m, l.ea, l.eb, r.ea, r.eb));
-    r.pad0 = r.pad1 = 0;
-    return r;
-  }
-};
-
-NBG_DEVICE i128 shfl_up_i128(i128 v, int d) {
+NBG_DEVICE i128 shfl_i128(i128 v, int src_or_delta, bool up) {
   const unsigned long long lo = static_cast<unsigned long long>(v);
   const unsigned long long hi = static_cast<unsigned long long>(v >> 64);
-  const unsigned long long rlo = __shfl_up_sync(0xffffffffu, lo, d);
-  const unsigned long long rhi = __shfl_up_sync(0xffffffffu, hi, d);
+  const unsigned long long rlo = up ? __shfl_up_sync(0xffffffffu, lo, src_or_delta) : __shfl_xor_sync(0xffffffffu, lo, src_or_delta);
+  const unsigned long long rhi = up ? __shfl_up_sync(0xffffffffu, hi, src_or_delta) : __shfl_xor_sync(0xffffffffu, hi, src_or_delta);
   return static_cast<i128>((static_cast<fx::u128>(rhi) << 64) | rlo);
 }
 
 template <int NS>
-NBG_DEVICE Sums<NS> shfl_up_sums(const Sums<NS>& v, int d) {
+NBG_DEVICE Sums<NS> shfl_sums(const Sums<NS>& v, int d, bool up) {
   Sums<NS> r;
 #pragma unroll
-  for (int j = 0; j < NS; ++j) r.s[j] = shfl_up_i128(v.s[j], d);
-  r.cnt = __shfl_up_sync(0xffffffffu, v.cnt, d);
-  r.inf_pos = __shfl_up_sync(0xffffffffu, v.inf_pos, d);
-  r.inf_neg = __shfl_up_sync(0xffffffffu, v.inf_neg, d);
-  r.inf_left = __shfl_up_sync(0xffffffffu, v.inf_left, d);
+  for (int j = 0; j < NS; ++j) r.s[j] = shfl_i128(v.s[j], d, up);
+  r.cnt = up ? __shfl_up_sync(0xffffffffu, v.cnt, d) : __shfl_xor_sync(0xffffffffu, v.cnt, d);
+  r.inf_pos = up ? __shfl_up_sync(0xffffffffu, v.inf_pos, d) : __shfl_xor_sync(0xffffffffu, v.inf_pos, d);
+  r.inf_neg = up ? __shfl_up_sync(0xffffffffu, v.inf_neg, d) : __shfl_xor_sync(0xffffffffu, v.inf_neg, d);
+  r.inf_left = up ? __shfl_up_sync(0xffffffffu, v.inf_left, d) : __shfl_xor_sync(0xffffffffu, v.inf_left, d);
   r.pad = 0;
   return r;
 }
 
-// |x| >= 2^512: the reference's x * x overflows to inf
-NBG_DEVICE bool square_overflows(double x) { return fx::biased_exponent(x) >= 1023 + 512; }
+// ---------------------------------------------------------------------------------
+// values from their bits (integer instructions only)
+// ---------------------------------------------------------------------------------
+struct Val {
+  unsigned long long m;  // integer mantissa: value = m * 2^(e - 1075)
+  int e;                 // biased float64 exponent, 1 for zeros and subnormals
+  bool neg, nan, inf;
+};
+NBG_DEVICE Val val_of(unsigned long long b) {  // float64 bits
+  const int eb = static_cast<int>((b >> 52) & 0x7ff);
+  Val v;
+  const unsigned long long f = b & 0x000fffffffffffffull;
+  v.m = f | (eb ? 0x0010000000000000ull : 0ull);
+  v.e = eb ? eb : 1;
+  v.neg = (b >> 63) != 0;
+  v.nan = eb == 0x7ff && f != 0;
+  v.inf = eb == 0x7ff && f == 0;
+  return v;
+}
+NBG_DEVICE Val val_of(unsigned b) {  // float32 bits, restated exactly in the float64 format
+  const int eb = static_cast<int>((b >> 23) & 0xff);
+  const unsigned f = b & 0x7fffffu;
+  Val v;
+  v.m = static_cast<unsigned long long>(f | (eb ? 0x800000u : 0u)) << 29;
+  v.e = eb ? eb + 896 : 897;
+  v.neg = (b >> 31) != 0;
+  v.nan = eb == 0xff && f != 0;
+  v.inf = eb == 0xff && f == 0;
+  return v;
+}
+
+NBG_DEVICE i128 fix_v(const Val& x, int E) {
+  const fx::u128 v = fx::shift_u(static_cast<fx::u128>(x.m), x.e - E + fx::kValueShift);
+  return x.neg ? -static_cast<i128>(v) : static_cast<i128>(v);
+}
+NBG_DEVICE i128 fix_sq(const Val& x, int E) {
+  return static_cast<i128>(fx::shift_u(static_cast<fx::u128>(x.m) * x.m, 2 * (x.e - E) + fx::kSquareShift));
+}
+NBG_DEVICE i128 fix_pr(const Val& x, const Val& y, int Ex, int Ey) {
+  const fx::u128 v = fx::shift_u(static_cast<fx::u128>(x.m) * y.m, (x.e - Ex) + (y.e - Ey) + fx::kSquareShift);
+  return (x.neg != y.neg) ? -static_cast<i128>(v) : static_cast<i128>(v);
+}
+
+// the reference's x * x overflows to inf: |x| >= 2^512
+NBG_DEVICE bool sq_overflow(const Val& x) { return x.e >= 1023 + 512; }
+
+// A position: valid (pairwise complete), "bad" (an infinity, or for the variance-like
+// statistics a value whose square overflows), and its exponents for the scale.
+template <int OP>
+struct Pos {
+  Val a, b;
+  bool valid, bad;
+};
+template <int OP, typename B>
+NBG_DEVICE Pos<OP> pos_of(B ab, B bb) {
+  constexpr bool TWO = Traits<OP>::TWO, VL = Traits<OP>::VARLIKE;
+  Pos<OP> p;
+  p.a = val_of(ab);
+  p.b = TWO ? val_of(bb) : p.a;
+  p.valid = !p.a.nan && !(TWO && p.b.nan);
+  p.bad = p.valid && (p.a.inf || (TWO && p.b.inf) || (VL && (sq_overflow(p.a) || (TWO && sq_overflow(p.b)))));
+  return p;
+}
 
 // Add (sign = +1, the entering value) or remove (sign = -1, the leaving value) one
-// position's contribution at the tile scale (Ea, Eb).
-template <int OP, typename T>
-NBG_DEVICE void accumulate(Sums<Traits<OP>::NS>& acc, T av, T bv, bool use, int sign, int Ea, int Eb) {
+// position's contribution at the scale (Ea, Eb).
+template <int OP>
+NBG_DEVICE void accumulate(Sums<Traits<OP>::NS>& acc, const Pos<OP>& p, int sign, int Ea, int Eb) {
   constexpr bool TWO = Traits<OP>::TWO;
-  bool valid = use && !is_nan(av);
-  if (TWO) valid = valid && !is_nan(bv);
-  if (!valid) return;
-  const double a = static_cast<double>(av);
-  const double b = TWO ? static_cast<double>(bv) : 0.0;
+  if (!p.valid) return;
   acc.cnt += sign;
-  bool inf = fx::is_inf(a) || (TWO && fx::is_inf(b));
-  if (Traits<OP>::VARLIKE) inf = inf || square_overflows(a) || (TWO && square_overflows(b));
-  if (inf) {
+  if (p.bad) {
     if (sign > 0) {
-      if (TWO || Traits<OP>::VARLIKE || a > 0) acc.inf_pos += 1; else acc.inf_neg += 1;
+      if (TWO || Traits<OP>::VARLIKE || !p.a.neg) acc.inf_pos += 1; else acc.inf_neg += 1;
     } else {
       acc.inf_left += 1;
     }
@@ -183,39 +228,66 @@ NBG_DEVICE void accumulate(Sums<Traits<OP>::NS>& acc, T av, T bv, bool use, int 
   }
   i128 m[5];
   if (OP == kSum || OP == kMean) {
-    m[0] = fx::fix_value(a, Ea);
+    m[0] = fix_v(p.a, Ea);
   } else if (OP == kVar || OP == kStd) {
-    m[0] = fx::fix_value(a, Ea);
-    m[1] = fx::fix_square(a, Ea);
+    m[0] = fix_v(p.a, Ea);
+    m[1] = fix_sq(p.a, Ea);
   } else {
-    m[0] = fx::fix_value(a, Ea);
-    m[1] = fx::fix_value(b, Eb);
-    m[2] = fx::fix_product(a, b, Ea, Eb);
+    m[0] = fix_v(p.a, Ea);
+    m[1] = fix_v(p.b, Eb);
+    m[2] = fix_pr(p.a, p.b, Ea, Eb);
     if (OP == kCorr) {
-      m[3] = fx::fix_square(a, Ea);
-      m[4] = fx::fix_square(b, Eb);
+      m[3] = fix_sq(p.a, Ea);
+      m[4] = fix_sq(p.b, Eb);
     }
   }
 #pragma unroll
   for (int j = 0; j < Traits<OP>::NS; ++j) acc.s[j] = sign > 0 ? acc.s[j] + m[j] : acc.s[j] - m[j];
 }
 
-constexpr int kRcpTable = 1024;
-
-// s / c for an integer count c >= 1, correctly rounded (non-finite s: plain division,
-// the correction step would turn inf into NaN)
-NBG_DEVICE double div_count(double s, long long c, const double* rcp) {
-  if (c < kRcpTable && isfinite(s)) {
-    const double r = rcp[c];
-    const double q0 = s * r;
-    const double e = fma(-q0, static_cast<double>(c), s);
-    return fma(e, r, q0);
+// v * 2^L rounded to the nearest float64 (ties to even), with integer instructions;
+// results outside the normal range go through the general conversion.
+NBG_DEVICE double to_f64(i128 v, int L) {
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  const fx::u128 a = neg ? static_cast<fx::u128>(-v) : static_cast<fx::u128>(v);
+  const int lz = fx::clz128(a);
+  const fx::u128 nrm = a << lz;  // leading one at bit 127
+  unsigned long long mant = static_cast<unsigned long long>(nrm >> 75);  // 53 bits
+  const fx::u128 rest = nrm & ((static_cast<fx::u128>(1) << 75) - 1);
+  const fx::u128 half = static_cast<fx::u128>(1) << 74;
+  int e = 127 - lz + L + 1023;  // biased exponent of the leading one
+  if (rest > half || (rest == half && (mant & 1))) {
+    if (++mant == (1ull << 53)) {
+      mant >>= 1;
+      ++e;
+    }
   }
-  return s / static_cast<double>(c);
+  if (e < 1 || e > 2046) return fx::to_double(v, L);
+  const unsigned long long bits = (static_cast<unsigned long long>(neg) << 63) |
+                                  (static_cast<unsigned long long>(e) << 52) | (mant & 0x000fffffffffffffull);
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
+NBG_DEVICE bool finite_bits(double x) {
+  return (static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+
+// 1/c from the table (correctly rounded), beyond it a division
+NBG_DEVICE double rcp_of(long long c, const double* __restrict__ rcp, long long rcp_n) {
+  return c <= rcp_n ? __ldg(rcp + c) : 1.0 / static_cast<double>(c);
+}
+// s / c correctly rounded (Markstein's correction of s * (1/c)); non-finite s divides
+NBG_DEVICE double div_count(double s, long long c, double r) {
+  if (!finite_bits(s)) return s / static_cast<double>(c);
+  const double q0 = s * r;
+  const double e = fma(-q0, static_cast<double>(c), s);
+  return fma(e, r, q0);
 }
 
 template <int OP>
-NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long long min_count, const double* rcp) {
+NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long long min_count,
+                           const double* __restrict__ rcp, long long rcp_n) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   const long long c = st.cnt;
   if (OP == kSum || OP == kMean) {
@@ -225,36 +297,36 @@ NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long 
     double s;
     if (st.inf_pos > 0) s = __longlong_as_double(0x7ff0000000000000ll);
     else if (st.inf_neg > 0) s = __longlong_as_double(static_cast<long long>(0xfff0000000000000ull));
-    else s = fx::to_double(st.s[0], fx::lsb_value(ea));
-    return OP == kSum ? s : div_count(s, c, rcp);
+    else s = to_f64(st.s[0], fx::lsb_value(ea));
+    return OP == kSum ? s : div_count(s, c, rcp_of(c, rcp, rcp_n));
   }
   if (OP == kVar || OP == kStd) {
     const long long mc = min_count > 2 ? min_count : 2;
     if (c < mc || st.inf_pos > 0) return nan;
-    const double s1 = fx::to_double(st.s[0], fx::lsb_value(ea));
-    const double s2 = fx::to_double(st.s[1], fx::lsb_product(ea, ea));
+    const double s1 = to_f64(st.s[0], fx::lsb_value(ea));
+    const double s2 = to_f64(st.s[1], fx::lsb_product(ea, ea));
     // (asum_sq - asum**2 / count) / (count - 1)    numbagg/moving.py:147-148
-    const double v = div_count(s2 - div_count(s1 * s1, c, rcp), c - 1, rcp);
+    const double v = (s2 - div_count(s1 * s1, c, rcp_of(c, rcp, rcp_n))) * rcp_of(c - 1, rcp, rcp_n);
     return OP == kStd ? sqrt(v) : v;
   }
   if (OP == kCov) {
     const long long mc = min_count > 2 ? min_count : 2;
     if (c < mc || st.inf_pos > 0) return nan;
-    const double sa = fx::to_double(st.s[0], fx::lsb_value(ea));
-    const double sb = fx::to_double(st.s[1], fx::lsb_value(eb));
-    const double sab = fx::to_double(st.s[2], fx::lsb_product(ea, eb));
+    const double sa = to_f64(st.s[0], fx::lsb_value(ea));
+    const double sb = to_f64(st.s[1], fx::lsb_value(eb));
+    const double sab = to_f64(st.s[2], fx::lsb_product(ea, eb));
     // (prodsum - asum * bsum / count) / (count - 1)   numbagg/moving.py:217-218
-    return div_count(sab - div_count(sa * sb, c, rcp), c - 1, rcp);
+    return (sab - div_count(sa * sb, c, rcp_of(c, rcp, rcp_n))) * rcp_of(c - 1, rcp, rcp_n);
   }
   // kCorr, numbagg/moving.py:263-273
   const long long mc = min_count > 1 ? min_count : 1;
   if (c < mc || st.inf_pos > 0) return nan;
-  const double sa = fx::to_double(st.s[0], fx::lsb_value(ea));
-  const double sb = fx::to_double(st.s[1], fx::lsb_value(eb));
-  const double sab = fx::to_double(st.s[2], fx::lsb_product(ea, eb));
-  const double saa = fx::to_double(st.s[3], fx::lsb_product(ea, ea));
-  const double sbb = fx::to_double(st.s[4], fx::lsb_product(eb, eb));
-  const double rc = c < kRcpTable ? rcp[c] : 1.0 / static_cast<double>(c);
+  const double sa = to_f64(st.s[0], fx::lsb_value(ea));
+  const double sb = to_f64(st.s[1], fx::lsb_value(eb));
+  const double sab = to_f64(st.s[2], fx::lsb_product(ea, eb));
+  const double saa = to_f64(st.s[3], fx::lsb_product(ea, ea));
+  const double sbb = to_f64(st.s[4], fx::lsb_product(eb, eb));
+  const double rc = rcp_of(c, rcp, rcp_n);
   const double avg_a = sa * rc;
   const double avg_b = sb * rc;
   const double var_a = saa * rc - avg_a * avg_a;
@@ -264,154 +336,195 @@ NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long 
   return vv > 0 ? cov_ab / sqrt(vv) : nan;
 }
 
+// ---------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------
 constexpr int NT = 256;
+constexpr int KT = 8;              // consecutive positions per thread
+constexpr int SUB = NT * KT;       // positions per sub-tile
+constexpr int SPAD = SUB + SUB / KT;
+constexpr long long kRcpEntries = 65536;
 
-// biased exponent of a finite valid value, 0 otherwise
-template <typename T>
-NBG_DEVICE int exp_of(T v, bool use) {
-  const double x = static_cast<double>(v);
-  return (use && !is_nan(v) && !fx::is_inf(x)) ? fx::biased_exponent(x) : 0;
+// padded stage index: one spare word after every thread's run of KT, so the 32
+// threads of a warp reading word k of their runs hit distinct banks
+NBG_DEVICE int spad(int p) { return p + p / KT; }
+
+template <int NS>
+NBG_DEVICE Sums<NS> block_sum(Sums<NS> v, Sums<NS>* warp_buf) {  // result valid in every thread
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = add(v, shfl_sums(v, o, false));
+  __syncthreads();
+  if (lane == 0) warp_buf[warp] = v;
+  __syncthreads();
+  Sums<NS> r = warp_buf[0];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) r = add(r, warp_buf[w]);
+  return r;
 }
 
-template <int OP, typename T, int K>
-__global__ void __launch_bounds__(NT) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
-                                                  T* __restrict__ out, long long rows, long long n,
-                                                  long long window, long long min_count,
-                                                  long long tiles_per_row, void* ws_base,
-                                                  size_t ws_bytes) {
+NBG_DEVICE int block_max(int v, int* buf) {  // result valid in every thread; buf[NT/32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(v)));
+  __syncthreads();
+  if (lane == 0) buf[warp] = v;
+  __syncthreads();
+  int r = buf[0];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) r = max(r, buf[w]);
+  return r;
+}
+
+template <int OP, typename T>
+__global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                     T* __restrict__ out, long long rows, long long n,
+                                                     long long window, long long min_count, long long chunk_len,
+                                                     long long chunks, const double* __restrict__ rcp,
+                                                     long long rcp_n, long long* __restrict__ first_bad) {
   constexpr int NS = Traits<OP>::NS;
   constexpr bool TWO = Traits<OP>::TWO;
-  constexpr long long TILE = static_cast<long long>(NT) * K;
+  typedef typename BitsOf<T>::type B;
   using S = Sums<NS>;
-  using X = XState<NS>;
-  __shared__ double rcp[kRcpTable];
-  __shared__ S warp_tot[NT / 32];
-  __shared__ X carry_smem;
-  __shared__ int emax_smem[2][NT / 32];
-  __shared__ long long tile_smem;
+  // stage (dynamic shared memory): entering a, leaving a[, entering b, leaving b]
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  B(*stage)[SPAD] = reinterpret_cast<B(*)[SPAD]>(stage_raw);
+  __shared__ S warp_buf[NT / 32];
+  __shared__ S carry_s;
+  __shared__ int red[2][NT / 32];
+  const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
+  const long long c0 = chunk * chunk_len, c1 = min(n, c0 + chunk_len);
+  const B* ar = as_bits(a) + row * n;
+  const B* br = TWO ? as_bits(b) + row * n : ar;
+  T* orow = out + row * n;
+  const unsigned long long last_use = l2_evict_first();
 
-  const long long total_tiles = rows * tiles_per_row;
-  Workspace ws = make_workspace(ws_base, ws_bytes);
-  const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
-  for (int c = threadIdx.x; c < kRcpTable; c += NT) rcp[c] = c ? 1.0 / static_cast<double>(c) : 0.0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // ---- the state entering the chunk: the window [c0 - w, c0) ----
+  const long long h0 = c0 > window ? c0 - window : 0;
+  int ea = 0, eb = 0;
+  for (long long i = h0 + tid; i < c0; i += NT) {
+    const Pos<OP> p = pos_of<OP>(ar[i], TWO ? br[i] : ar[i]);
+    if (p.valid && !p.bad) {
+      ea = max(ea, p.a.e);
+      eb = max(eb, p.b.e);
+    }
+  }
+  int Ea = max(1, block_max(ea, red[0]));
+  int Eb = TWO ? max(1, block_max(eb, red[1])) : 1;
+  S seed = zero_sums<NS>();
+  for (long long i = h0 + tid; i < c0; i += NT)
+    accumulate<OP>(seed, pos_of<OP>(ar[i], TWO ? br[i] : ar[i]), +1, Ea, Eb);
+  seed = block_sum(seed, warp_buf);
+  if (tid == 0) carry_s = seed;
 
-  for (;;) {
-    if (threadIdx.x == 0) tile_smem = claim_tile(ws.hdr);
-    __syncthreads();
-    const long long tile = tile_smem;
-    if (tile >= total_tiles) break;
-    const TileCoord tc = tile_coord(tile, rows);
-    const long long row = tc.row, chunk = tc.chunk;
-    const long long p0 = chunk * TILE + static_cast<long long>(threadIdx.x) * K;
-    const T* ar = a + row * n;
-    const T* br = TWO ? b + row * n : nullptr;
-
-    T av[K], bv[K], ao[K], bo[K];
-    int ea = 0, eb = 0;
+  long long bad_pos = LLONG_MAX;
+  for (long long s0 = c0; s0 < c1; s0 += SUB) {
+    // ---- stage the entering and leaving values; the sub-tile's exponents ----
+    int ma = 0, mb = 0;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      const bool in = i < n;
-      const bool has_old = in && i >= window;
-      av[k] = in ? ar[i] : T(0);
-      ao[k] = has_old ? ar[i - window] : T(0);
-      bv[k] = (TWO && in) ? br[i] : T(0);
-      bo[k] = (TWO && has_old) ? br[i - window] : T(0);
-      ea = max(ea, max(exp_of(av[k], in), exp_of(ao[k], has_old)));
-      if (TWO) eb = max(eb, max(exp_of(bv[k], in), exp_of(bo[k], has_old)));
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      const long long i = s0 + p;
+      const bool in = i < c1, old = in && i >= window;
+      const B xa = in ? ar[i] : nanb;
+      const B xo = old ? ld_hint(ar + (i - window), last_use) : nanb;
+      const B ya = (TWO && in) ? br[i] : nanb;
+      const B yo = (TWO && old) ? ld_hint(br + (i - window), last_use) : nanb;
+      stage[0][spad(p)] = xa;
+      stage[1][spad(p)] = xo;
+      if (TWO) {
+        stage[2][spad(p)] = ya;
+        stage[3][spad(p)] = yo;
+      }
+      const Pos<OP> pe = pos_of<OP>(xa, ya), po = pos_of<OP>(xo, yo);
+      if (pe.valid && !pe.bad) {
+        ma = max(ma, pe.a.e);
+        mb = max(mb, pe.b.e);
+      }
+      if (po.valid && !po.bad) {
+        ma = max(ma, po.a.e);
+        mb = max(mb, po.b.e);
+      }
+      if (pe.bad) bad_pos = min(bad_pos, i);
     }
-    // tile scale: block-wide maximum exponent
-    ea = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(ea)));
-    eb = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(eb)));
-    if (lane == 0) {
-      emax_smem[0][warp] = ea;
-      emax_smem[1][warp] = eb;
-    }
-    __syncthreads();
-    ea = 1;
-    eb = 1;
-#pragma unroll
-    for (int w = 0; w < NT / 32; ++w) {
-      ea = max(ea, emax_smem[0][w]);
-      eb = max(eb, emax_smem[1][w]);
-    }
+    const int Ean = max(Ea, block_max(ma, red[0]));  // the syncs also publish the stage
+    const int Ebn = TWO ? max(Eb, block_max(mb, red[1])) : Eb;
+    S carry = rescale<OP>(carry_s, Ea, Eb, Ean, Ebn);
+    Ea = Ean;
+    Eb = Ebn;
 
-    // ---- pass 1: thread-serial sum of the differences ----
-    S run = zero_sums<NS>();
+    // ---- thread totals over KT consecutive positions, block scan ----
+    const int q0 = tid * KT;
+    S tot = zero_sums<NS>();
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      accumulate<OP, T>(run, av[k], bv[k], i < n, +1, ea, eb);
-      accumulate<OP, T>(run, ao[k], bo[k], i < n && i >= window, -1, ea, eb);
+    for (int k = 0; k < KT; ++k) {
+      const int sp = spad(q0 + k);
+      accumulate<OP>(tot, pos_of<OP>(stage[0][sp], TWO ? stage[2][sp] : stage[0][sp]), +1, Ea, Eb);
+      accumulate<OP>(tot, pos_of<OP>(stage[1][sp], TWO ? stage[3][sp] : stage[1][sp]), -1, Ea, Eb);
     }
-    // ---- block scan of thread totals (exact, one scale) ----
-    S incl = run;
+    S incl = tot;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const S up = shfl_up_sums(incl, d);
+      const S up = shfl_sums(incl, d, true);
       if (lane >= d) incl = add(up, incl);
     }
-    if (lane == 31) warp_tot[warp] = incl;
+    if (lane == 31) warp_buf[warp] = incl;
     __syncthreads();
-    if (warp == 0) {
-      S wt = lane < NT / 32 ? warp_tot[lane] : zero_sums<NS>();
+    S st = carry;
 #pragma unroll
-      for (int d = 1; d < NT / 32; d <<= 1) {
-        const S up = shfl_up_sums(wt, d);
-        if (lane >= d) wt = add(up, wt);
-      }
-      if (lane < NT / 32) warp_tot[lane] = wt;
-    }
-    __syncthreads();
-    S lane_excl = shfl_up_sums(incl, 1);
-    if (lane == 0) lane_excl = zero_sums<NS>();
-    const S thread_excl = warp ? add(warp_tot[warp - 1], lane_excl) : lane_excl;
+    for (int w = 0; w < NT / 32; ++w)
+      if (w < warp) st = add(st, warp_buf[w]);
+    S lane_excl = shfl_sums(incl, 1, true);
+    if (lane > 0) st = add(st, lane_excl);
 
-    // ---- carry into the tile: decoupled look-back (warp 0) ----
-    if (warp == 0) {
-      X agg;
-      agg.m = warp_tot[NT / 32 - 1];
-      agg.ea = ea;
-      agg.eb = eb;
-      agg.pad0 = agg.pad1 = 0;
-      const CombineOp<OP> op;
-      if (chunk == 0) {
-        if (lane == 0) {
-          if (tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
-          carry_smem = op.identity();
-        }
-      } else {
-        if (lane == 0) publish(ws, tile, epoch, kStateAggregate, agg);
-        __syncwarp();
-        bool ok;
-        const X carry = warp_lookback<X>(ws, tile, chunk, rows, epoch, op, ok);
-        if (lane == 0) {
-          publish(ws, tile, epoch, kStatePrefix, op.combine(carry, agg));
-          carry_smem = carry;
-        }
-      }
-    }
-    __syncthreads();
-    // output scale: the larger of the carry's and the tile's
-    const X carry = carry_smem;
-    const int eo_a = max(carry.ea, ea), eo_b = max(carry.eb, eb);
-    S st = add(rescale<OP>(carry.m, carry.ea, carry.eb, eo_a, eo_b), rescale<OP>(thread_excl, ea, eb, eo_a, eo_b));
-
-    // ---- pass 2: outputs ----
-    T* orow = out + row * n;
+    // ---- outputs, written back over the thread's own entering slots ----
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const long long i = p0 + k;
-      S d = zero_sums<NS>();
-      accumulate<OP, T>(d, av[k], bv[k], i < n, +1, ea, eb);
-      accumulate<OP, T>(d, ao[k], bo[k], i < n && i >= window, -1, ea, eb);
-      st = add(st, rescale<OP>(d, ea, eb, eo_a, eo_b));
-      if (i < n) orow[i] = static_cast<T>(finalize<OP>(st, eo_a, eo_b, min_count, rcp));
+    for (int k = 0; k < KT; ++k) {
+      const int sp = spad(q0 + k);
+      accumulate<OP>(st, pos_of<OP>(stage[0][sp], TWO ? stage[2][sp] : stage[0][sp]), +1, Ea, Eb);
+      accumulate<OP>(st, pos_of<OP>(stage[1][sp], TWO ? stage[3][sp] : stage[1][sp]), -1, Ea, Eb);
+      const T r = static_cast<T>(finalize<OP>(st, Ea, Eb, min_count, rcp, rcp_n));
+      if (sizeof(T) == 8) stage[0][sp] = static_cast<B>(__double_as_longlong(static_cast<double>(r)));
+      else stage[0][sp] = static_cast<B>(__float_as_uint(static_cast<float>(r)));
     }
-    __syncthreads();  // shared state is reused by the next tile
+    if (tid == NT - 1) carry_s = st;  // everyone read carry_s before the scan's barrier
+    __syncthreads();
+    B* ob = as_bits(orow);
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      if (s0 + p < c1) ob[s0 + p] = stage[0][spad(p)];
+    }
+    __syncthreads();
   }
-  if (threadIdx.x == 0) finish_cta(ws.hdr);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bad_pos = min(bad_pos, __shfl_xor_sync(0xffffffffu, bad_pos, o));
+  if (lane == 0 && bad_pos != LLONG_MAX) atomicMin(reinterpret_cast<unsigned long long*>(first_bad + row),
+                                                   static_cast<unsigned long long>(bad_pos));
+}
+
+// reciprocal table and per-row first infinity, once per call
+__global__ void move_setup_kernel(double* __restrict__ rcp, long long rcp_n, long long* __restrict__ first_bad,
+                                  long long rows) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const long long t0 = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (long long c = t0; c <= rcp_n; c += stride) rcp[c] = c ? 1.0 / static_cast<double>(c) : 0.0;
+  for (long long r = t0; r < rows; r += stride) first_bad[r] = LLONG_MAX;
+}
+
+// The reference never recovers from an infinity (inf - inf = NaN in its running sums):
+// NaN from the first position where one has left the window (sum, mean) or entered it.
+template <typename T, bool VARLIKE>
+__global__ void move_poison_kernel(T* __restrict__ out, long long rows, long long n, long long window,
+                                   const long long* __restrict__ first_bad) {
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    const long long f = first_bad[r];
+    if (f == LLONG_MAX) continue;
+    const long long from = VARLIKE ? f : (f > LLONG_MAX - window ? LLONG_MAX : f + window);
+    const T nan = quiet_nan(T(0));
+    for (long long i = (from < n ? from : n) + threadIdx.x; i < n; i += blockDim.x) out[r * n + i] = nan;
+  }
 }
 
 }  // namespace moving
@@ -424,19 +537,25 @@ using namespace nbg;
 using namespace nbg::moving;
 
 namespace {
-constexpr int kItemsPerThread = 8;
 
-long long tiles_per_row_for(long long n) {
-  const long long tile = static_cast<long long>(NT) * kItemsPerThread;
-  return n <= 0 ? 0 : (n + tile - 1) / tile;
+long long rcp_entries(long long n) { return n < kRcpEntries ? n : kRcpEntries; }
+
+size_t move_scratch_bytes(long long rows, long long n) {
+  return 256 + static_cast<size_t>(rcp_entries(n) + 1) * 8 + 256 + static_cast<size_t>(rows) * 8;
 }
 
-int grid_for(long long total_tiles) {
+// Chunks of at least 8 windows (the seed re-reads one window per chunk), 16 sub-tiles
+// at least; smaller when the grid would not fill the GPU.
+long long chunk_len_for(long long rows, long long n, long long window) {
+  const long long w8 = (window > (LLONG_MAX / 16) ? LLONG_MAX / 16 : window) * 8;
+  long long len = std::max<long long>(16LL * SUB, ((w8 + SUB - 1) / SUB) * SUB);
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long cap = static_cast<long long>(sms) * 8;
-  return static_cast<int>(total_tiles < cap ? total_tiles : cap);
+  const long long want = 4LL * 2 * sms;  // CTAs: four waves of two per SM
+  while (len > SUB && rows * ((n + len - 1) / len) < want)
+    len = std::max<long long>(SUB, ((len / 2 + SUB - 1) / SUB) * SUB);
+  return len;
 }
 
 template <int OP, typename T>
@@ -445,21 +564,34 @@ int launch_move(const T* a, const T* b, T* out, long long rows, long long n, lon
   if (rows < 0 || n < 0 || window <= 0 || min_count < 0) return kInvalidArgument;
   if (rows == 0 || n == 0) return kOk;
   if (!a || !out || (Traits<OP>::TWO && !b)) return kInvalidArgument;
-  const long long tpr = tiles_per_row_for(n);
-  const long long total = rows * tpr;
-  if (!ws || ws_bytes < workspace_bytes(total)) return kWorkspaceTooSmall;
-  move_kernel<OP, T, kItemsPerThread><<<grid_for(total), NT, 0, stream>>>(
-      a, b, out, rows, n, window, min_count, tpr, ws, ws_bytes);
-  note_launches(1);
+  if (!ws || ws_bytes < move_scratch_bytes(rows, n)) return kWorkspaceTooSmall;
+  unsigned char* base = static_cast<unsigned char*>(ws);
+  base = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(base) + 255) & ~static_cast<size_t>(255));
+  const long long rcp_n = rcp_entries(n);
+  double* rcp = reinterpret_cast<double*>(base);
+  long long* first_bad = reinterpret_cast<long long*>(
+      (reinterpret_cast<size_t>(base + (rcp_n + 1) * 8) + 255) & ~static_cast<size_t>(255));
+  const long long len = chunk_len_for(rows, n, window);
+  const long long chunks = (n + len - 1) / len;
+  if (rows * chunks > 0x7fffffffLL) return kUnsupported;
+  const long long setup_items = std::max(rcp_n + 1, rows);
+  move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
+      rcp, rcp_n, first_bad, rows);
+  const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
+  auto kern = move_kernel<OP, T>;
+  if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  kern<<<static_cast<int>(rows * chunks), NT, smem, stream>>>(a, b, out, rows, n, window, min_count, len, chunks, rcp,
+                                                              rcp_n, first_bad);
+  move_poison_kernel<T, Traits<OP>::VARLIKE><<<static_cast<int>(std::min<long long>(rows, 4096)), 256, 0, stream>>>(
+      out, rows, n, window, first_bad);
+  note_launches(3);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 }  // namespace
 
 extern "C" {
 
-size_t nbg_move_workspace_bytes(long long rows, long long n) {
-  return workspace_bytes(rows * tiles_per_row_for(n));
-}
+size_t nbg_move_workspace_bytes(long long rows, long long n) { return move_scratch_bytes(rows, n); }
 
 #define NBG_MOVE1(NAME, OPC, T, SFX)                                                        \
   int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window,  \

@@ -63,7 +63,7 @@ def _move(name: str, arrs, window, min_count, axis):
     out = torch.empty((rows, n), dtype=dtype, device=a.device)
     if out.numel():
         L = _lib.lib()
-        ws = _lib.workspaces.scan(L.nbg_move_workspace_bytes(rows, n), a.device)
+        ws = _lib.workspaces.scratch(L.nbg_move_workspace_bytes(rows, n), a.device)
         fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
         args = [f.data_ptr() for f in flats] + [
             out.data_ptr(),
