@@ -551,6 +551,17 @@ def scan_inputs(device, cols):
     return a, b, small, X
 
 
+class _Fp32c:
+    """The package with precision="fp32c" added to every call."""
+
+    def __init__(self, nb):
+        self._nb = nb
+
+    def __getattr__(self, name):
+        f = getattr(self._nb, name)
+        return lambda *args, **kw: f(*args, precision="fp32c", **kw)
+
+
 def scan_calls(cols):
     """(key, callable(nb, a, b, small, X), algorithmic bytes, elements) of the scan suite.
     min_count = window // 2: with 2% NaN the default (= window) leaves almost every
@@ -569,6 +580,9 @@ def scan_calls(cols):
         out.append(
             (f"move_exp_nancorr_a{al:g}", lambda nb, a, b, s, X, al=al: nb.move_exp_nancorr(a, b, alpha=al), 24 * R * N, R * N)
         )
+    # the FP32-compensated forms of the same calls
+    for key, fn, nbytes, elems in list(out):
+        out.append((key + "_fp32c", lambda nb, a, b, s, X, fn=fn: fn(_Fp32c(nb), a, b, s, X), nbytes, elems))
     T, V = MATRIX_T, MATRIX_V
     for f in ("move_covmatrix", "move_corrmatrix"):
         out.append((f"{f}_w500", lambda nb, a, b, s, X, f=f: getattr(nb, f)(X, window=500, min_count=400), 4 * T * V + 4 * T * V * V, T * V))
@@ -638,8 +652,14 @@ def run_scan_suite(args):
             "GB/s": round(nbytes / (us / 1e6) / 1e9, 1),
             "note": "16 MB, L2-resident; 1000 launches replayed from CUDA graphs",
         }
+    speedup = {
+        k[: -len("_fp32c")]: round(per_func[k[: -len("_fp32c")]]["ms"] / v["ms"], 2)
+        for k, v in per_func.items()
+        if k.endswith("_fp32c") and k[: -len("_fp32c")] in per_func
+    }
     line = {
         "suite": "scan",
+        "fp32c_speedup": speedup,
         "unit": "GB/s",
         "peak": peak,
         "peak_kind": peak_kind,

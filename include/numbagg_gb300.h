@@ -8,14 +8,14 @@
  * device pointers for data, `stream` is a cudaStream_t (NULL = legacy default).
  * Calls are asynchronous on `stream`; every call returns an NBG_* status.
  *
- * Workspaces.  Moving windows and fills carry state between tiles through a
- * look-back workspace sized by nbg_move_workspace_bytes() / nbg_fill_workspace_bytes().
+ * Workspaces.  Fills carry state between tiles through a look-back workspace sized by
+ * nbg_fill_workspace_bytes().
  * A look-back workspace must be zero-filled once when it is allocated; it then
  * maintains itself across launches.  One workspace per stream: launches that share
- * it must be ordered on one stream.  The exponential moving functions and the grouped
- * reductions take a scratch buffer (nbg_move_exp_workspace_bytes(),
- * nbg_group_workspace_bytes()) that needs no initialisation; do not share a scratch
- * buffer with a look-back workspace.
+ * it must be ordered on one stream.  Moving windows, the exponential moving functions
+ * and the grouped reductions take a scratch buffer (nbg_move_workspace_bytes(),
+ * nbg_move_exp_workspace_bytes(), nbg_group_workspace_bytes()) that needs no
+ * initialisation; do not share a scratch buffer with a look-back workspace.
  */
 #ifndef NUMBAGG_GB300_H
 #define NUMBAGG_GB300_H
@@ -65,7 +65,9 @@ NBG_API int nbg_debug_lookback_timeout(void* ws, size_t ws_bytes, int spin_limit
  *   move_var  numbagg/moving.py:154-181    move_std  numbagg/moving.py:123-151
  *   move_cov  numbagg/moving.py:184-220    move_corr numbagg/moving.py:223-275
  * signature "(a),(),()->(a)" / "(a),(a),(),()->(a)"; a, b, out: rows x n.
- * min_count is passed unclamped (each kernel applies the reference's max()). */
+ * min_count is passed unclamped (each kernel applies the reference's max()).
+ * ws: a scratch buffer of nbg_move_workspace_bytes(rows, n) bytes, no initialisation
+ * needed (reciprocal table and per-row state, rewritten by every call). */
 NBG_API size_t nbg_move_workspace_bytes(long long rows, long long n);
 #define NBG_DECL_MOVE1(NAME, T, SFX)                                                      \
   NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window, \
@@ -86,6 +88,15 @@ NBG_DECL_MOVE2(move_cov, double, f64)
 NBG_DECL_MOVE2(move_cov, float, f32)
 NBG_DECL_MOVE2(move_corr, double, f64)
 NBG_DECL_MOVE2(move_corr, float, f32)
+/* FP32-compensated forms of the float64 entry points (no reference counterpart: numbagg
+ * computes in float64 only).  The same exact window sums, finalised from exact integer
+ * numerators in double-float on the FP32 pipes; about 2^-46 relative error. */
+NBG_DECL_MOVE1(move_sum, double, f64_fp32c)
+NBG_DECL_MOVE1(move_mean, double, f64_fp32c)
+NBG_DECL_MOVE1(move_var, double, f64_fp32c)
+NBG_DECL_MOVE1(move_std, double, f64_fp32c)
+NBG_DECL_MOVE2(move_cov, double, f64_fp32c)
+NBG_DECL_MOVE2(move_corr, double, f64_fp32c)
 
 /* ---- exponentially weighted moving functions ---------------------------------------
  * Replaces the gufuncs built by ndmoveexp (numbagg/decorators.py:344-414) from
@@ -120,6 +131,17 @@ NBG_DECL_EXP2(move_exp_nancov, double, f64)
 NBG_DECL_EXP2(move_exp_nancov, float, f32)
 NBG_DECL_EXP2(move_exp_nancorr, double, f64)
 NBG_DECL_EXP2(move_exp_nancorr, float, f32)
+/* FP32-compensated forms of the float64 entry points (no reference counterpart):
+ * the same deterministic scan in double-float on the FP32 pipes, about 2^-46 relative
+ * precision per operation; variance, standard deviation, covariance and correlation
+ * subtract each row's first finite value first (they are shift invariant). */
+NBG_DECL_EXP1(move_exp_nancount, double, f64_fp32c)
+NBG_DECL_EXP1(move_exp_nanmean, double, f64_fp32c)
+NBG_DECL_EXP1(move_exp_nansum, double, f64_fp32c)
+NBG_DECL_EXP1(move_exp_nanvar, double, f64_fp32c)
+NBG_DECL_EXP1(move_exp_nanstd, double, f64_fp32c)
+NBG_DECL_EXP2(move_exp_nancov, double, f64_fp32c)
+NBG_DECL_EXP2(move_exp_nancorr, double, f64_fp32c)
 
 /* ---- fills --------------------------------------------------------------------------
  * Replaces the gufuncs built by ndfill (numbagg/decorators.py:417-487) from

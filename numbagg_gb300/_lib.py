@@ -76,6 +76,15 @@ def _declare(lib: ctypes.CDLL) -> None:
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
         for f in ("move_covmatrix", "move_corrmatrix"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
+    # FP32-compensated forms of the float64 scans
+    for f in ("move_sum", "move_mean", "move_var", "move_std"):
+        sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+    for f in ("move_cov", "move_corr"):
+        sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+    for f in ("move_exp_nancount", "move_exp_nanmean", "move_exp_nansum", "move_exp_nanvar", "move_exp_nanstd"):
+        sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
+    for f in ("move_exp_nancov", "move_exp_nancorr"):
+        sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
     for dt in ("f64", "f32", "i32", "i64"):
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)

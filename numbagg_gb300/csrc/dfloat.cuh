@@ -1,0 +1,255 @@
+// Double-float arithmetic on the FP32 pipes, for the FP32-compensated ("fp32c") forms.
+//
+// A df is hi + lo with |lo| <= ulp(hi) / 2: about 48 significant bits from two
+// float32 words, computed with the error-free transformations
+//   TwoSum     (Knuth, The Art of Computer Programming vol. 2, 4.2.2),
+//   FastTwoSum (Dekker, Numer. Math. 18, 1971),
+//   TwoProduct with a fused multiply-add (Ogita, Rump and Oishi, SIAM J. Sci. Comput.
+//   26(6), 2005),
+// and the double-float add, multiply, divide and square root of Hida, Li and Bailey's
+// QD library paper (ARITH-15, 2001; square root by Karp's method).  Every operation is
+// an explicitly rounded float32 intrinsic, so the compiler cannot contract it.
+//
+// An sdf ("scaled df") keeps the exponent apart: value = m * 2^e with m a df in
+// [1, 2) (or zero), so results never leave float32's exponent range; finalisations
+// built from exact integer sums go integer -> sdf -> float64 without touching the
+// FP64 pipe, which on this GPU accepts one warp instruction per 16 cycles.
+#pragma once
+
+#include "fixed128.cuh"
+
+namespace nbg {
+namespace dfl {
+
+struct df {
+  float hi, lo;
+};
+
+NBG_DEVICE df two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return df{s, e};
+}
+NBG_DEVICE df fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return df{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+NBG_DEVICE df two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return df{p, __fmaf_rn(a, b, -p)};
+}
+NBG_DEVICE df df_add(df x, df y) {  // the accurate ("IEEE") double-float sum
+  df s = two_sum(x.hi, y.hi);
+  const df t = two_sum(x.lo, y.lo);
+  float e = __fadd_rn(s.lo, t.hi);
+  s = fast_two_sum(s.hi, e);
+  e = __fadd_rn(t.lo, s.lo);
+  return fast_two_sum(s.hi, e);
+}
+NBG_DEVICE df df_neg(df x) { return df{-x.hi, -x.lo}; }
+NBG_DEVICE df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+NBG_DEVICE df df_mul(df x, df y) {
+  const df p = two_prod(x.hi, y.hi);
+  const float e = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo));
+  return fast_two_sum(p.hi, e);
+}
+NBG_DEVICE df df_mul_f(df x, float y) {
+  const df p = two_prod(x.hi, y);
+  return fast_two_sum(p.hi, __fmaf_rn(x.lo, y, p.lo));
+}
+NBG_DEVICE df df_div(df x, df y) {  // three-quotient long division
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  df r = df_sub(x, df_mul_f(y, q1));
+  const float q2 = __fdiv_rn(r.hi, y.hi);
+  r = df_sub(r, df_mul_f(y, q2));
+  const float q3 = __fdiv_rn(r.hi, y.hi);
+  return df_add(fast_two_sum(q1, q2), df{q3, 0.0f});
+}
+NBG_DEVICE df df_sqrt(df a) {  // a > 0; Karp: sqrt(a) ~ a*x + (a - (a*x)^2) * x / 2, x = 1/sqrt(a)
+  const float x = __frsqrt_rn(a.hi);
+  const float ax = __fmul_rn(a.hi, x);
+  const df d = df_sub(a, two_prod(ax, ax));
+  return fast_two_sum(ax, __fmul_rn(d.hi, __fmul_rn(x, 0.5f)));
+}
+
+// ---- scaled double-float ------------------------------------------------------------
+struct sdf {
+  df m;       // in [1, 2) or zero, sign in m
+  int e;      // value = m * 2^e
+  bool zero;
+};
+
+NBG_DEVICE float pow2f(int k) {  // 2^k for -126 <= k <= 127
+  return __int_as_float((k + 127) << 23);
+}
+
+// renormalise m into [1, 2) (m nonzero and finite)
+NBG_DEVICE sdf sdf_norm(df m, int e) {
+  const int k = ((__float_as_int(m.hi) >> 23) & 0xff) - 127;  // exponent of hi
+  const float s = pow2f(-k);
+  sdf r;
+  r.m = df{__fmul_rn(m.hi, s), __fmul_rn(m.lo, s)};
+  r.e = e + k;
+  r.zero = false;
+  return r;
+}
+
+// |u| (a nonzero 128-bit magnitude) * 2^L as an sdf, sign given
+NBG_DEVICE sdf sdf_from_u128(fx::u128 a, int L, bool neg) {
+  sdf r;
+  if (a == 0) {
+    r.m = df{0.0f, 0.0f};
+    r.e = 0;
+    r.zero = true;
+    return r;
+  }
+  const int lz = fx::clz128(a);
+  const fx::u128 n = a << lz;  // leading one at bit 127
+  // hi: bits 127..104 (24 bits), lo: the next 24 bits, both truncated (48-bit value)
+  const unsigned hm = static_cast<unsigned>(n >> 104);
+  const unsigned lm = static_cast<unsigned>(n >> 80) & 0xffffffu;
+  const float hi = __uint2float_rn(hm) * pow2f(-23);            // in [1, 2)
+  const float lo = __uint2float_rn(lm) * pow2f(-47);            // exact: 24 bits
+  df m = fast_two_sum(hi, lo);  // may round up to exactly 2
+  if (neg) m = df_neg(m);
+  return sdf_norm(m, (127 - lz) + L);
+}
+
+NBG_DEVICE sdf sdf_div(const sdf& x, const sdf& y) {  // y nonzero
+  if (x.zero) return x;
+  return sdf_norm(df_div(x.m, y.m), x.e - y.e);
+}
+NBG_DEVICE sdf sdf_mul(const sdf& x, const sdf& y) {
+  if (x.zero) return x;
+  if (y.zero) return y;
+  return sdf_norm(df_mul(x.m, y.m), x.e + y.e);
+}
+NBG_DEVICE sdf sdf_sqrt(const sdf& x) {  // x >= 0
+  if (x.zero) return x;
+  df m = x.m;
+  int e = x.e;
+  if (e & 1) {  // make the exponent even: m in [2, 4)
+    m = df{__fmul_rn(m.hi, 2.0f), __fmul_rn(m.lo, 2.0f)};
+    e -= 1;
+  }
+  return sdf_norm(df_sqrt(m), e / 2);
+}
+// an integer count as an sdf (exact below 2^48)
+NBG_DEVICE sdf sdf_from_count(long long c) {
+  return sdf_from_u128(static_cast<fx::u128>(c), 0, false);
+}
+
+// float64 nearest to x (hi + lo exactly combined, then rounded once), integer only
+NBG_DEVICE double sdf_to_f64(const sdf& x) {
+  if (x.zero) return 0.0;
+  // both words as signed 64-bit integers scaled by 2^62 relative to 2^e, summed exactly
+  const unsigned hb = static_cast<unsigned>(__float_as_int(x.m.hi));
+  const unsigned lb = static_cast<unsigned>(__float_as_int(x.m.lo));
+  const bool neg = (hb >> 31) != 0;
+  const int eh = static_cast<int>((hb >> 23) & 0xff) - 127;  // 0 after normalisation
+  long long vh = static_cast<long long>((hb & 0x7fffffu) | 0x800000u) << (62 - 23 + eh);
+  long long vl = 0;
+  if ((lb & 0x7fffffffu) != 0) {
+    const int el = static_cast<int>((lb >> 23) & 0xff) - 127;
+    const long long ml = static_cast<long long>((lb & 0x7fffffu) | 0x800000u);
+    const int sh = 62 - 23 + el;
+    vl = sh >= 0 ? (ml << sh) : (sh > -64 ? (ml >> -sh) : 0);
+    if ((lb >> 31) != (hb >> 31)) vl = -vl;
+  }
+  const long long v = vh + vl;  // |v| < 2^63, sign of hi
+  return fx::to_f64(static_cast<fx::i128>(neg ? -v : v), x.e - 62);
+}
+
+// ---- 256-bit integers for exact moment numerators ------------------------------------
+struct u256 {
+  unsigned long long w[4];  // little-endian words
+};
+
+NBG_DEVICE u256 mul128(fx::u128 a, fx::u128 b) {
+  const unsigned long long a0 = static_cast<unsigned long long>(a), a1 = static_cast<unsigned long long>(a >> 64);
+  const unsigned long long b0 = static_cast<unsigned long long>(b), b1 = static_cast<unsigned long long>(b >> 64);
+  const fx::u128 p00 = static_cast<fx::u128>(a0) * b0;
+  const fx::u128 p01 = static_cast<fx::u128>(a0) * b1;
+  const fx::u128 p10 = static_cast<fx::u128>(a1) * b0;
+  const fx::u128 p11 = static_cast<fx::u128>(a1) * b1;
+  u256 r;
+  r.w[0] = static_cast<unsigned long long>(p00);
+  fx::u128 mid = (p00 >> 64) + static_cast<unsigned long long>(p01) + static_cast<unsigned long long>(p10);
+  r.w[1] = static_cast<unsigned long long>(mid);
+  fx::u128 hi = (mid >> 64) + (p01 >> 64) + (p10 >> 64) + p11;
+  r.w[2] = static_cast<unsigned long long>(hi);
+  r.w[3] = static_cast<unsigned long long>(hi >> 64);
+  return r;
+}
+NBG_DEVICE u256 shl256(u256 x, int s) {  // 0 <= s < 64
+  if (s == 0) return x;
+  u256 r;
+  r.w[3] = (x.w[3] << s) | (x.w[2] >> (64 - s));
+  r.w[2] = (x.w[2] << s) | (x.w[1] >> (64 - s));
+  r.w[1] = (x.w[1] << s) | (x.w[0] >> (64 - s));
+  r.w[0] = x.w[0] << s;
+  return r;
+}
+NBG_DEVICE u256 shl256_words(u256 x, int words) {
+  u256 r = {{0, 0, 0, 0}};
+  for (int i = 3; i >= words; --i) r.w[i] = x.w[i - words];
+  return r;
+}
+NBG_DEVICE bool ge256(const u256& a, const u256& b) {
+  for (int i = 3; i >= 0; --i)
+    if (a.w[i] != b.w[i]) return a.w[i] > b.w[i];
+  return true;
+}
+NBG_DEVICE u256 sub256(const u256& a, const u256& b) {  // a >= b
+  u256 r;
+  unsigned long long borrow = 0;
+  for (int i = 0; i < 4; ++i) {
+    const unsigned long long t = a.w[i] - b.w[i];
+    const unsigned long long b1 = a.w[i] < b.w[i];
+    r.w[i] = t - borrow;
+    borrow = b1 | (t < borrow);
+  }
+  return r;
+}
+
+// |x| * 2^L as an sdf (48 leading bits, truncated below)
+NBG_DEVICE sdf sdf_from_u256(const u256& x, int L, bool neg) {
+  int top = 3;
+  while (top > 0 && x.w[top] == 0) --top;
+  if (x.w[top] == 0) return sdf_from_u128(0, 0, false);
+  // take the two words ending at `top` as a 128-bit window
+  const fx::u128 win = (static_cast<fx::u128>(x.w[top]) << 64) | (top > 0 ? x.w[top - 1] : 0ull);
+  return sdf_from_u128(win, L + 64 * (top - 1), neg);
+}
+
+// s * v for a signed 128-bit s and a magnitude v: sign and 256-bit magnitude
+struct s256 {
+  u256 mag;
+  bool neg;
+};
+NBG_DEVICE s256 smul(fx::i128 a, fx::i128 b) {
+  const bool na = a < 0, nb = b < 0;
+  const fx::u128 ua = na ? static_cast<fx::u128>(-a) : static_cast<fx::u128>(a);
+  const fx::u128 ub = nb ? static_cast<fx::u128>(-b) : static_cast<fx::u128>(b);
+  return s256{mul128(ua, ub), na != nb};
+}
+// x - y for signed 256-bit values
+NBG_DEVICE s256 ssub(const s256& x, const s256& y) {
+  if (x.neg != y.neg) {  // magnitudes add
+    u256 r;
+    unsigned long long carry = 0;
+    for (int i = 0; i < 4; ++i) {
+      const unsigned long long t = x.mag.w[i] + y.mag.w[i];
+      const unsigned long long c1 = t < x.mag.w[i];
+      r.w[i] = t + carry;
+      carry = c1 | (r.w[i] < t);
+    }
+    return s256{r, x.neg};
+  }
+  if (ge256(x.mag, y.mag)) return s256{sub256(x.mag, y.mag), x.neg};
+  return s256{sub256(y.mag, x.mag), !x.neg};
+}
+
+}  // namespace dfl
+}  // namespace nbg

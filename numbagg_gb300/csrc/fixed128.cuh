@@ -97,5 +97,29 @@ NBG_DEVICE double to_double(i128 v, int L) {
   return neg ? -d : d;
 }
 
+// v * 2^L rounded to the nearest float64 (ties to even), with integer instructions;
+// results outside the normal range go through the general conversion.
+NBG_DEVICE double to_f64(i128 v, int L) {
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  const u128 a = neg ? static_cast<u128>(-v) : static_cast<u128>(v);
+  const int lz = clz128(a);
+  const u128 nrm = a << lz;  // leading one at bit 127
+  unsigned long long mant = static_cast<unsigned long long>(nrm >> 75);  // 53 bits
+  const u128 rest = nrm & ((static_cast<u128>(1) << 75) - 1);
+  const u128 half = static_cast<u128>(1) << 74;
+  int e = 127 - lz + L + 1023;  // biased exponent of the leading one
+  if (rest > half || (rest == half && (mant & 1))) {
+    if (++mant == (1ull << 53)) {
+      mant >>= 1;
+      ++e;
+    }
+  }
+  if (e < 1 || e > 2046) return to_double(v, L);
+  const unsigned long long bits = (static_cast<unsigned long long>(neg) << 63) |
+                                  (static_cast<unsigned long long>(e) << 52) | (mant & 0x000fffffffffffffull);
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
 }  // namespace fx
 }  // namespace nbg

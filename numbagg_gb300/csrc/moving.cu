@@ -41,6 +41,7 @@
 // second kernel writes the NaNs after it.  Accumulation is exact for float32 arrays
 // too (numba keeps float64 accumulators there, numbagg/moving.py:16); the result is
 // rounded to float32.
+#include "dfloat.cuh"
 #include "fixed128.cuh"
 
 #include <algorithm>
@@ -245,30 +246,6 @@ NBG_DEVICE void accumulate(Sums<Traits<OP>::NS>& acc, const Pos<OP>& p, int sign
   for (int j = 0; j < Traits<OP>::NS; ++j) acc.s[j] = sign > 0 ? acc.s[j] + m[j] : acc.s[j] - m[j];
 }
 
-// v * 2^L rounded to the nearest float64 (ties to even), with integer instructions;
-// results outside the normal range go through the general conversion.
-NBG_DEVICE double to_f64(i128 v, int L) {
-  if (v == 0) return 0.0;
-  const bool neg = v < 0;
-  const fx::u128 a = neg ? static_cast<fx::u128>(-v) : static_cast<fx::u128>(v);
-  const int lz = fx::clz128(a);
-  const fx::u128 nrm = a << lz;  // leading one at bit 127
-  unsigned long long mant = static_cast<unsigned long long>(nrm >> 75);  // 53 bits
-  const fx::u128 rest = nrm & ((static_cast<fx::u128>(1) << 75) - 1);
-  const fx::u128 half = static_cast<fx::u128>(1) << 74;
-  int e = 127 - lz + L + 1023;  // biased exponent of the leading one
-  if (rest > half || (rest == half && (mant & 1))) {
-    if (++mant == (1ull << 53)) {
-      mant >>= 1;
-      ++e;
-    }
-  }
-  if (e < 1 || e > 2046) return fx::to_double(v, L);
-  const unsigned long long bits = (static_cast<unsigned long long>(neg) << 63) |
-                                  (static_cast<unsigned long long>(e) << 52) | (mant & 0x000fffffffffffffull);
-  return __longlong_as_double(static_cast<long long>(bits));
-}
-
 NBG_DEVICE bool finite_bits(double x) {
   return (static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
 }
@@ -297,14 +274,14 @@ NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long 
     double s;
     if (st.inf_pos > 0) s = __longlong_as_double(0x7ff0000000000000ll);
     else if (st.inf_neg > 0) s = __longlong_as_double(static_cast<long long>(0xfff0000000000000ull));
-    else s = to_f64(st.s[0], fx::lsb_value(ea));
+    else s = fx::to_f64(st.s[0], fx::lsb_value(ea));
     return OP == kSum ? s : div_count(s, c, rcp_of(c, rcp, rcp_n));
   }
   if (OP == kVar || OP == kStd) {
     const long long mc = min_count > 2 ? min_count : 2;
     if (c < mc || st.inf_pos > 0) return nan;
-    const double s1 = to_f64(st.s[0], fx::lsb_value(ea));
-    const double s2 = to_f64(st.s[1], fx::lsb_product(ea, ea));
+    const double s1 = fx::to_f64(st.s[0], fx::lsb_value(ea));
+    const double s2 = fx::to_f64(st.s[1], fx::lsb_product(ea, ea));
     // (asum_sq - asum**2 / count) / (count - 1)    numbagg/moving.py:147-148
     const double v = (s2 - div_count(s1 * s1, c, rcp_of(c, rcp, rcp_n))) * rcp_of(c - 1, rcp, rcp_n);
     return OP == kStd ? sqrt(v) : v;
@@ -312,20 +289,20 @@ NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long 
   if (OP == kCov) {
     const long long mc = min_count > 2 ? min_count : 2;
     if (c < mc || st.inf_pos > 0) return nan;
-    const double sa = to_f64(st.s[0], fx::lsb_value(ea));
-    const double sb = to_f64(st.s[1], fx::lsb_value(eb));
-    const double sab = to_f64(st.s[2], fx::lsb_product(ea, eb));
+    const double sa = fx::to_f64(st.s[0], fx::lsb_value(ea));
+    const double sb = fx::to_f64(st.s[1], fx::lsb_value(eb));
+    const double sab = fx::to_f64(st.s[2], fx::lsb_product(ea, eb));
     // (prodsum - asum * bsum / count) / (count - 1)   numbagg/moving.py:217-218
     return (sab - div_count(sa * sb, c, rcp_of(c, rcp, rcp_n))) * rcp_of(c - 1, rcp, rcp_n);
   }
   // kCorr, numbagg/moving.py:263-273
   const long long mc = min_count > 1 ? min_count : 1;
   if (c < mc || st.inf_pos > 0) return nan;
-  const double sa = to_f64(st.s[0], fx::lsb_value(ea));
-  const double sb = to_f64(st.s[1], fx::lsb_value(eb));
-  const double sab = to_f64(st.s[2], fx::lsb_product(ea, eb));
-  const double saa = to_f64(st.s[3], fx::lsb_product(ea, ea));
-  const double sbb = to_f64(st.s[4], fx::lsb_product(eb, eb));
+  const double sa = fx::to_f64(st.s[0], fx::lsb_value(ea));
+  const double sb = fx::to_f64(st.s[1], fx::lsb_value(eb));
+  const double sab = fx::to_f64(st.s[2], fx::lsb_product(ea, eb));
+  const double saa = fx::to_f64(st.s[3], fx::lsb_product(ea, ea));
+  const double sbb = fx::to_f64(st.s[4], fx::lsb_product(eb, eb));
   const double rc = rcp_of(c, rcp, rcp_n);
   const double avg_a = sa * rc;
   const double avg_b = sb * rc;
@@ -334,6 +311,59 @@ NBG_DEVICE double finalize(const Sums<Traits<OP>::NS>& st, int ea, int eb, long 
   const double cov_ab = sab * rc - avg_a * avg_b;
   const double vv = var_a * var_b;
   return vv > 0 ? cov_ab / sqrt(vv) : nan;
+}
+
+// The FP32-compensated ("fp32c") finalisation: no floating-point rounding until the
+// last step.  The second moments are exact integer numerators
+//     N_xy = c * S_xy * 2^93 - S_x * S_y        (256-bit, units of 2^(Lx + Ly))
+// so var = N_xx / (c (c - 1)), cov = N_xy / (c (c - 1)), corr = N_ab / sqrt(N_aa N_bb)
+// (the reference's formulas with the common factors cancelled), evaluated in scaled
+// double-float on the FP32 pipes and rounded once to float64.  About 2^-46 relative
+// error, and no cancellation: the result is that of the exact window sums.
+NBG_DEVICE dfl::s256 numerator(i128 sxy, i128 sx, i128 sy, long long c) {
+  dfl::s256 a = dfl::smul(sxy, static_cast<i128>(c));
+  a.mag = dfl::shl256(dfl::shl256_words(a.mag, 1), 29);  // * 2^93
+  return dfl::ssub(a, dfl::smul(sx, sy));
+}
+
+template <int OP>
+NBG_DEVICE double finalize_c(const Sums<Traits<OP>::NS>& st, int ea, int eb, long long min_count) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const long long c = st.cnt;
+  if (OP == kSum || OP == kMean) {
+    const long long mc = OP == kMean ? (min_count > 1 ? min_count : 1) : min_count;
+    if (c < mc) return nan;
+    if (st.inf_left > 0 || (st.inf_pos > 0 && st.inf_neg > 0)) return nan;
+    if (st.inf_pos > 0) return __longlong_as_double(0x7ff0000000000000ll);
+    if (st.inf_neg > 0) return __longlong_as_double(static_cast<long long>(0xfff0000000000000ull));
+    if (OP == kSum) return fx::to_f64(st.s[0], fx::lsb_value(ea));
+    const i128 s1 = st.s[0];
+    const dfl::sdf m = dfl::sdf_from_u128(s1 < 0 ? static_cast<fx::u128>(-s1) : static_cast<fx::u128>(s1),
+                                          fx::lsb_value(ea), s1 < 0);
+    return dfl::sdf_to_f64(dfl::sdf_div(m, dfl::sdf_from_count(c)));
+  }
+  if (OP == kVar || OP == kStd || OP == kCov) {
+    const long long mc = min_count > 2 ? min_count : 2;
+    if (c < mc || st.inf_pos > 0) return nan;
+    const dfl::s256 nm = OP == kCov ? numerator(st.s[2], st.s[0], st.s[1], c) : numerator(st.s[1], st.s[0], st.s[0], c);
+    const int L = fx::lsb_value(ea) + fx::lsb_value(OP == kCov ? eb : ea);
+    const dfl::sdf v = dfl::sdf_div(dfl::sdf_from_u256(nm.mag, L, nm.neg), dfl::sdf_from_count(c * (c - 1)));
+    if (OP == kStd) return nm.neg ? nan : dfl::sdf_to_f64(dfl::sdf_sqrt(v));
+    return dfl::sdf_to_f64(v);
+  }
+  // kCorr
+  const long long mc = min_count > 1 ? min_count : 1;
+  if (c < mc || st.inf_pos > 0) return nan;
+  const dfl::s256 nab = numerator(st.s[2], st.s[0], st.s[1], c);
+  const dfl::s256 naa = numerator(st.s[3], st.s[0], st.s[0], c);
+  const dfl::s256 nbb = numerator(st.s[4], st.s[1], st.s[1], c);
+  const int la = fx::lsb_value(ea), lb = fx::lsb_value(eb);
+  const dfl::sdf vaa = dfl::sdf_from_u256(naa.mag, 2 * la, naa.neg);
+  const dfl::sdf vbb = dfl::sdf_from_u256(nbb.mag, 2 * lb, nbb.neg);
+  if (vaa.zero || vbb.zero || naa.neg != nbb.neg) return nan;  // var_a * var_b > 0
+  const dfl::sdf den = dfl::sdf_sqrt(dfl::sdf_mul(vaa, vbb));
+  const dfl::sdf cov = dfl::sdf_from_u256(nab.mag, la + lb, nab.neg);
+  return dfl::sdf_to_f64(dfl::sdf_div(cov, den));
 }
 
 // ---------------------------------------------------------------------------------
@@ -375,7 +405,7 @@ NBG_DEVICE int block_max(int v, int* buf) {  // result valid in every thread; bu
   return r;
 }
 
-template <int OP, typename T>
+template <int OP, typename T, bool C>
 __global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
                                                      T* __restrict__ out, long long rows, long long n,
                                                      long long window, long long min_count, long long chunk_len,
@@ -484,7 +514,7 @@ __global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, co
       const int sp = spad(q0 + k);
       accumulate<OP>(st, pos_of<OP>(stage[0][sp], TWO ? stage[2][sp] : stage[0][sp]), +1, Ea, Eb);
       accumulate<OP>(st, pos_of<OP>(stage[1][sp], TWO ? stage[3][sp] : stage[1][sp]), -1, Ea, Eb);
-      const T r = static_cast<T>(finalize<OP>(st, Ea, Eb, min_count, rcp, rcp_n));
+      const T r = static_cast<T>(C ? finalize_c<OP>(st, Ea, Eb, min_count) : finalize<OP>(st, Ea, Eb, min_count, rcp, rcp_n));
       if (sizeof(T) == 8) stage[0][sp] = static_cast<B>(__double_as_longlong(static_cast<double>(r)));
       else stage[0][sp] = static_cast<B>(__float_as_uint(static_cast<float>(r)));
     }
@@ -558,7 +588,7 @@ long long chunk_len_for(long long rows, long long n, long long window) {
   return len;
 }
 
-template <int OP, typename T>
+template <int OP, typename T, bool C>
 int launch_move(const T* a, const T* b, T* out, long long rows, long long n, long long window,
                 long long min_count, void* ws, size_t ws_bytes, cudaStream_t stream) {
   if (rows < 0 || n < 0 || window <= 0 || min_count < 0) return kInvalidArgument;
@@ -578,7 +608,7 @@ int launch_move(const T* a, const T* b, T* out, long long rows, long long n, lon
   move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
       rcp, rcp_n, first_bad, rows);
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
-  auto kern = move_kernel<OP, T>;
+  auto kern = move_kernel<OP, T, C>;
   if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   kern<<<static_cast<int>(rows * chunks), NT, smem, stream>>>(a, b, out, rows, n, window, min_count, len, chunks, rcp,
                                                               rcp_n, first_bad);
@@ -593,31 +623,39 @@ extern "C" {
 
 size_t nbg_move_workspace_bytes(long long rows, long long n) { return move_scratch_bytes(rows, n); }
 
-#define NBG_MOVE1(NAME, OPC, T, SFX)                                                        \
+#define NBG_MOVE1(NAME, OPC, T, SFX, C)                                                        \
   int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window,  \
                          long long min_count, void* ws, size_t ws_bytes, void* stream) {     \
-    return launch_move<OPC, T>(a, nullptr, out, rows, n, window, min_count, ws, ws_bytes,    \
+    return launch_move<OPC, T, C>(a, nullptr, out, rows, n, window, min_count, ws, ws_bytes, \
                                static_cast<cudaStream_t>(stream));                          \
   }
-#define NBG_MOVE2(NAME, OPC, T, SFX)                                                        \
+#define NBG_MOVE2(NAME, OPC, T, SFX, C)                                                        \
   int nbg_##NAME##_##SFX(const T* a, const T* b, T* out, long long rows, long long n,        \
                          long long window, long long min_count, void* ws, size_t ws_bytes,   \
                          void* stream) {                                                    \
-    return launch_move<OPC, T>(a, b, out, rows, n, window, min_count, ws, ws_bytes,          \
+    return launch_move<OPC, T, C>(a, b, out, rows, n, window, min_count, ws, ws_bytes,       \
                                static_cast<cudaStream_t>(stream));                          \
   }
 
-NBG_MOVE1(move_sum, kSum, double, f64)
-NBG_MOVE1(move_sum, kSum, float, f32)
-NBG_MOVE1(move_mean, kMean, double, f64)
-NBG_MOVE1(move_mean, kMean, float, f32)
-NBG_MOVE1(move_var, kVar, double, f64)
-NBG_MOVE1(move_var, kVar, float, f32)
-NBG_MOVE1(move_std, kStd, double, f64)
-NBG_MOVE1(move_std, kStd, float, f32)
-NBG_MOVE2(move_cov, kCov, double, f64)
-NBG_MOVE2(move_cov, kCov, float, f32)
-NBG_MOVE2(move_corr, kCorr, double, f64)
-NBG_MOVE2(move_corr, kCorr, float, f32)
+NBG_MOVE1(move_sum, kSum, double, f64, false)
+NBG_MOVE1(move_sum, kSum, float, f32, false)
+NBG_MOVE1(move_mean, kMean, double, f64, false)
+NBG_MOVE1(move_mean, kMean, float, f32, false)
+NBG_MOVE1(move_var, kVar, double, f64, false)
+NBG_MOVE1(move_var, kVar, float, f32, false)
+NBG_MOVE1(move_std, kStd, double, f64, false)
+NBG_MOVE1(move_std, kStd, float, f32, false)
+NBG_MOVE2(move_cov, kCov, double, f64, false)
+NBG_MOVE2(move_cov, kCov, float, f32, false)
+NBG_MOVE2(move_corr, kCorr, double, f64, false)
+NBG_MOVE2(move_corr, kCorr, float, f32, false)
+// FP32-compensated forms (float64 arrays): the same exact window sums, finalised in
+// scaled double-float (no reference counterpart; numbagg computes in float64 only)
+NBG_MOVE1(move_sum, kSum, double, f64_fp32c, true)
+NBG_MOVE1(move_mean, kMean, double, f64_fp32c, true)
+NBG_MOVE1(move_var, kVar, double, f64_fp32c, true)
+NBG_MOVE1(move_std, kStd, double, f64_fp32c, true)
+NBG_MOVE2(move_cov, kCov, double, f64_fp32c, true)
+NBG_MOVE2(move_corr, kCorr, double, f64_fp32c, true)
 
 }  // extern "C"

@@ -1,24 +1,32 @@
 // Exponentially weighted family move_exp_nan{count,mean,sum,var,std,cov,corr}
-// (numbagg/moving_exp.py:12-335), float64 and float32 arrays.
+// (numbagg/moving_exp.py:12-335), float64 and float32 arrays, plus FP32-compensated
+// ("fp32c") forms of the float64 entry points.
 //
 // Each reference state variable follows s_i = decay_i * s_{i-1} + b_i, where
 // decay_i = 1 - alpha_i and b_i is the contribution of position i (zero when the
 // value is NaN); sum_weight_2 decays by decay_i**2.  A position is therefore an
 // affine map s -> A*s + B, and maps compose associatively:
 //     (A2, B2) o (A1, B1) = (A2*A1, A2*B1 + B2).
-// A row is cut into tiles.  Phase 0 composes each tile's map (thread-serial over K
-// positions, then a fixed-structure warp-shuffle scan); phase 1 scans the tile maps
-// of each row in a fixed order to get the state entering every tile; phase 2 replays
-// each position with the reference's own update, a rounded multiply followed by a
-// rounded add (no FMA), starting from that state, and finalises with the reference's
-// formulas.  The composition order never depends on timing, so results are
-// bit-identical run to run and a prefix of a row gives the same bits as the whole
-// row.  Phase 0 and 2 both read the input; the plain float64 form is bound by the
-// FP64 pipe (about 1.6 adds per clock per SM on GB300), not by that extra read.
+// A row is cut into tiles of 1024 positions.  Phase 0 composes each tile's map
+// (thread-serial over 8 consecutive positions, then a fixed-structure warp-shuffle
+// scan); phase 1 scans the tile maps of each row in a fixed order to get the state
+// entering every tile; phase 2 replays each position with the reference's update (a
+// rounded multiply followed by a rounded add, no FMA) from that state, and finalises
+// with the reference's formulas.  The composition order never depends on timing, so
+// results are bit-identical run to run and a prefix of a row gives the same bits as
+// the whole row.  Values, alphas and outputs pass through a padded shared stage so
+// that every global access of a warp is one contiguous run.
+//
+// The arithmetic is a policy: F64 is the reference's float64 (bound by this GPU's
+// FP64 pipe, one warp instruction per 16 cycles); DF is double-float on the FP32
+// pipes (dfloat.cuh, about 48 bits).  The DF forms of the shift-invariant statistics
+// (variance, standard deviation, covariance, correlation) first subtract a per-row
+// pivot, the row's first finite value, from every value, so data such as 1e6 + N(0,1)
+// keeps its significant digits; the mean and the sums need no pivot.
 //
 // alpha: a scalar, a 1-D array along the scanned axis shared by every row, or one
 // value per element (numbagg/decorators.py:398-409).
-#include "nbg_common.cuh"
+#include "dfloat.cuh"
 
 namespace nbg {
 namespace mexp {
@@ -27,99 +35,166 @@ enum Op : int { kCount = 0, kMean, kSum, kVar, kStd, kCov, kCorr };
 
 template <int OP>
 struct Traits;
-// state order and decay kind per op; kW2 marks the sum_weight_2 state (decay**2)
+// state order and decay kind per op; W2 marks the sum_weight_2 state (decay**2)
 template <>
-struct Traits<kCount> { static constexpr int NS = 2; static constexpr bool TWO = false; static constexpr int W2 = -1; };
+struct Traits<kCount> { static constexpr int NS = 2; static constexpr bool TWO = false; static constexpr int W2 = -1; static constexpr bool PIVOT = false; };
 template <>
-struct Traits<kMean> { static constexpr int NS = 3; static constexpr bool TWO = false; static constexpr int W2 = -1; };
+struct Traits<kMean> { static constexpr int NS = 3; static constexpr bool TWO = false; static constexpr int W2 = -1; static constexpr bool PIVOT = false; };
 template <>
-struct Traits<kSum> { static constexpr int NS = 2; static constexpr bool TWO = false; static constexpr int W2 = -1; };
+struct Traits<kSum> { static constexpr int NS = 2; static constexpr bool TWO = false; static constexpr int W2 = -1; static constexpr bool PIVOT = false; };
 template <>
-struct Traits<kVar> { static constexpr int NS = 5; static constexpr bool TWO = false; static constexpr int W2 = 3; };
+struct Traits<kVar> { static constexpr int NS = 5; static constexpr bool TWO = false; static constexpr int W2 = 3; static constexpr bool PIVOT = true; };
 template <>
-struct Traits<kStd> { static constexpr int NS = 5; static constexpr bool TWO = false; static constexpr int W2 = 3; };
+struct Traits<kStd> { static constexpr int NS = 5; static constexpr bool TWO = false; static constexpr int W2 = 3; static constexpr bool PIVOT = true; };
 template <>
-struct Traits<kCov> { static constexpr int NS = 6; static constexpr bool TWO = true; static constexpr int W2 = 4; };
+struct Traits<kCov> { static constexpr int NS = 6; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
 template <>
-struct Traits<kCorr> { static constexpr int NS = 8; static constexpr bool TWO = true; static constexpr int W2 = 4; };
+struct Traits<kCorr> { static constexpr int NS = 8; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
 
-template <int NS>
+// ---------------------------------------------------------------------------------
+// arithmetic policies
+// ---------------------------------------------------------------------------------
+struct F64 {
+  typedef double T;
+  static constexpr bool kDF = false;
+  static NBG_DEVICE T zero() { return 0.0; }
+  static NBG_DEVICE T one() { return 1.0; }
+  static NBG_DEVICE T mul(T a, T b) { return __dmul_rn(a, b); }
+  static NBG_DEVICE T add(T a, T b) { return __dadd_rn(a, b); }
+  static NBG_DEVICE T sub(T a, T b) { return __dsub_rn(a, b); }
+  static NBG_DEVICE T fma(T a, T b, T c) { return ::fma(a, b, c); }
+};
+
+NBG_DEVICE dfl::df df_from_f64(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0x000fffffffffffffull;
+  if (e == 0x7ff) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u | (m ? 0x400000u : 0u))), 0.0f};
+  const int E = e - 1023;
+  if (e == 0 || E < -126) {  // below float32's normal range: a float32 rounding of it
+    const float h = __double2float_rn(x);
+    return dfl::df{h, __double2float_rn(x - static_cast<double>(h))};
+  }
+  if (E > 127) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u)), 0.0f};
+  const unsigned long long M = m | 0x0010000000000000ull;
+  const float hi = __int_as_float(static_cast<int>(sign | (static_cast<unsigned>(E + 127) << 23) |
+                                                  static_cast<unsigned>((M >> 29) & 0x7fffffu)));
+  const unsigned rem = static_cast<unsigned>(M & ((1ull << 29) - 1));
+  float lo = 0.0f;
+  if (rem && E - 52 >= -126) {
+    lo = __fmul_rn(__uint2float_rn(rem), dfl::pow2f(E - 52));
+    if (sign) lo = -lo;
+  }
+  return dfl::fast_two_sum(hi, lo);
+}
+
+NBG_DEVICE double df_to_f64(dfl::df x) {
+  const unsigned hb = static_cast<unsigned>(__float_as_int(x.hi));
+  if (((hb >> 23) & 0xff) == 0xff) {  // inf or NaN
+    const unsigned long long s = static_cast<unsigned long long>(hb >> 31) << 63;
+    return __longlong_as_double(static_cast<long long>(s | 0x7ff0000000000000ull | ((hb & 0x7fffffu) ? (1ull << 51) : 0ull)));
+  }
+  if ((hb & 0x7fffffffu) == 0) return x.lo == 0.0f ? __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(hb >> 31) << 63)) : static_cast<double>(x.lo);
+  return dfl::sdf_to_f64(dfl::sdf_norm(x, 0));
+}
+
+struct DF {
+  typedef dfl::df T;
+  static constexpr bool kDF = true;
+  static NBG_DEVICE T zero() { return dfl::df{0.0f, 0.0f}; }
+  static NBG_DEVICE T one() { return dfl::df{1.0f, 0.0f}; }
+  static NBG_DEVICE T mul(T a, T b) { return dfl::df_mul(a, b); }
+  static NBG_DEVICE T add(T a, T b) { return dfl::df_add(a, b); }
+  static NBG_DEVICE T sub(T a, T b) { return dfl::df_sub(a, b); }
+  static NBG_DEVICE T fma(T a, T b, T c) { return dfl::df_add(dfl::df_mul(a, b), c); }
+};
+
+// a value of the array as the policy's number (float64 policy: exact widening)
+NBG_DEVICE double value_as(F64, unsigned long long bits) { return __longlong_as_double(static_cast<long long>(bits)); }
+NBG_DEVICE double value_as(F64, unsigned bits) { return static_cast<double>(__int_as_float(static_cast<int>(bits))); }
+NBG_DEVICE dfl::df value_as(DF, unsigned long long bits) { return df_from_f64(__longlong_as_double(static_cast<long long>(bits))); }
+NBG_DEVICE dfl::df value_as(DF, unsigned bits) { return dfl::df{__int_as_float(static_cast<int>(bits)), 0.0f}; }
+NBG_DEVICE double as_f64(double x) { return x; }
+NBG_DEVICE double as_f64(dfl::df x) { return df_to_f64(x); }
+NBG_DEVICE dfl::df as_num(DF, double x) { return df_from_f64(x); }
+NBG_DEVICE double as_num(F64, double x) { return x; }
+
+template <int NS, typename N>
 struct Map {
-  double A1, A2;  // product of decays, product of squared decays
-  double B[NS];
-  int seen;       // any valid value (move_exp_nansum's zero_count flag)
+  typename N::T A1, A2;  // product of decays, product of squared decays
+  typename N::T B[NS];
+  int seen;  // any valid value (move_exp_nansum's zero_count flag)
   int pad;
 };
 
-template <int OP>
-NBG_DEVICE Map<Traits<OP>::NS> identity_map() {
-  Map<Traits<OP>::NS> m;
-  m.A1 = 1.0;
-  m.A2 = 1.0;
+template <int OP, typename N>
+NBG_DEVICE Map<Traits<OP>::NS, N> identity_map() {
+  Map<Traits<OP>::NS, N> m;
+  m.A1 = N::one();
+  m.A2 = N::one();
 #pragma unroll
-  for (int j = 0; j < Traits<OP>::NS; ++j) m.B[j] = 0.0;
+  for (int j = 0; j < Traits<OP>::NS; ++j) m.B[j] = N::zero();
   m.seen = 0;
   m.pad = 0;
   return m;
 }
 
 // later o earlier
-template <int OP>
-NBG_DEVICE Map<Traits<OP>::NS> compose(const Map<Traits<OP>::NS>& earlier, const Map<Traits<OP>::NS>& later) {
-  Map<Traits<OP>::NS> r;
-  r.A1 = later.A1 * earlier.A1;
-  r.A2 = later.A2 * earlier.A2;
+template <int OP, typename N>
+NBG_DEVICE Map<Traits<OP>::NS, N> compose(const Map<Traits<OP>::NS, N>& earlier, const Map<Traits<OP>::NS, N>& later) {
+  Map<Traits<OP>::NS, N> r;
+  r.A1 = N::mul(later.A1, earlier.A1);
+  r.A2 = N::mul(later.A2, earlier.A2);
 #pragma unroll
   for (int j = 0; j < Traits<OP>::NS; ++j) {
-    const double a = (j == Traits<OP>::W2) ? later.A2 : later.A1;
-    r.B[j] = fma(a, earlier.B[j], later.B[j]);
+    const typename N::T a = (j == Traits<OP>::W2) ? later.A2 : later.A1;
+    r.B[j] = N::fma(a, earlier.B[j], later.B[j]);
   }
   r.seen = earlier.seen | later.seen;
   r.pad = 0;
   return r;
 }
 
-template <int OP>
-struct ComposeOp {
-  NBG_DEVICE Map<Traits<OP>::NS> identity() const { return identity_map<OP>(); }
-  NBG_DEVICE Map<Traits<OP>::NS> combine(const Map<Traits<OP>::NS>& e, const Map<Traits<OP>::NS>& l) const {
-    return compose<OP>(e, l);
-  }
-};
+NBG_DEVICE double shfl_up_num(double v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+NBG_DEVICE dfl::df shfl_up_num(dfl::df v, int d) {
+  return dfl::df{__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
+}
 
-template <int OP>
-NBG_DEVICE Map<Traits<OP>::NS> shfl_up_map(const Map<Traits<OP>::NS>& v, int d) {
-  Map<Traits<OP>::NS> r;
-  r.A1 = __shfl_up_sync(0xffffffffu, v.A1, d);
-  r.A2 = __shfl_up_sync(0xffffffffu, v.A2, d);
+template <int OP, typename N>
+NBG_DEVICE Map<Traits<OP>::NS, N> shfl_up_map(const Map<Traits<OP>::NS, N>& v, int d) {
+  Map<Traits<OP>::NS, N> r;
+  r.A1 = shfl_up_num(v.A1, d);
+  r.A2 = shfl_up_num(v.A2, d);
 #pragma unroll
-  for (int j = 0; j < Traits<OP>::NS; ++j) r.B[j] = __shfl_up_sync(0xffffffffu, v.B[j], d);
+  for (int j = 0; j < Traits<OP>::NS; ++j) r.B[j] = shfl_up_num(v.B[j], d);
   r.seen = __shfl_up_sync(0xffffffffu, v.seen, d);
   r.pad = 0;
   return r;
 }
 
 // contributions b_j of one position, in the reference's state order
-template <int OP>
-NBG_DEVICE void contributions(double x, double y, double alpha, double* b) {
+template <int OP, typename N>
+NBG_DEVICE void contributions(typename N::T x, typename N::T y, typename N::T alpha, typename N::T* b) {
+  const typename N::T one = N::one();
   if (OP == kCount) {  // count, weight
-    b[0] = 1.0; b[1] = alpha;
+    b[0] = one; b[1] = alpha;
   } else if (OP == kMean) {  // numer, denom, weight
-    b[0] = x; b[1] = 1.0; b[2] = alpha;
+    b[0] = x; b[1] = one; b[2] = alpha;
   } else if (OP == kSum) {  // numer, weight
     b[0] = x; b[1] = alpha;
   } else if (OP == kVar || OP == kStd) {  // sum_x_2, sum_x, sum_weight, sum_weight_2, weight
-    b[0] = __dmul_rn(x, x); b[1] = x; b[2] = 1.0; b[3] = 1.0; b[4] = alpha;
+    b[0] = N::mul(x, x); b[1] = x; b[2] = one; b[3] = one; b[4] = alpha;
   } else if (OP == kCov) {  // sum_x1, sum_x2, sum_x1x2, sum_weight, sum_weight_2, weight
-    b[0] = x; b[1] = y; b[2] = __dmul_rn(x, y); b[3] = 1.0; b[4] = 1.0; b[5] = alpha;
+    b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one; b[5] = alpha;
   } else {  // kCorr: + sum_x1_2, sum_x2_2
-    b[0] = x; b[1] = y; b[2] = __dmul_rn(x, y); b[3] = 1.0; b[4] = 1.0; b[5] = alpha;
-    b[6] = __dmul_rn(x, x); b[7] = __dmul_rn(y, y);
+    b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one; b[5] = alpha;
+    b[6] = N::mul(x, x); b[7] = N::mul(y, y);
   }
 }
 
 template <int OP>
-NBG_DEVICE double finalize(const double* s, int seen, double min_weight) {
+NBG_DEVICE double finalize(F64, const double* s, int seen, double min_weight) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   if (OP == kCount) return s[1] >= min_weight ? s[0] : nan;
   if (OP == kMean) return s[2] >= min_weight ? __ddiv_rn(s[0], s[1]) : nan;
@@ -154,59 +229,154 @@ NBG_DEVICE double finalize(const double* s, int seen, double min_weight) {
   return nan;
 }
 
+// double-float comparisons
+NBG_DEVICE bool df_pos(dfl::df x) { return x.hi > 0.0f || (x.hi == 0.0f && x.lo > 0.0f); }
+NBG_DEVICE bool df_ge(dfl::df x, double y) {  // x >= y (y a float64 constant of the call)
+  const dfl::df d = dfl::df_sub(x, df_from_f64(y));
+  return d.hi > 0.0f || (d.hi == 0.0f && d.lo >= 0.0f);
+}
+NBG_DEVICE dfl::df df_div0(dfl::df x, dfl::df y) {  // x / y with IEEE zeros, infinities and NaN
+  if (y.hi == 0.0f || !isfinite(y.hi) || !isfinite(x.hi)) return dfl::df{__fdiv_rn(x.hi, y.hi), 0.0f};
+  if (x.hi == 0.0f) return dfl::df{0.0f, 0.0f};
+  return dfl::df_div(x, y);
+}
+
+// The reference's formulas in double-float (the statistics that see pivoted values are
+// invariant under the shift).
+template <int OP>
+NBG_DEVICE double finalize(DF, const dfl::df* s, int seen, double min_weight) {
+  using namespace dfl;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const df one{1.0f, 0.0f};
+  if (OP == kCount) return df_ge(s[1], min_weight) ? df_to_f64(s[0]) : nan;
+  if (OP == kMean) return df_ge(s[2], min_weight) ? df_to_f64(df_div0(s[0], s[1])) : nan;
+  if (OP == kSum) return (df_ge(s[1], min_weight) && seen) ? df_to_f64(s[0]) : nan;
+  if (OP == kVar || OP == kStd) {
+    const df m = df_div0(s[1], s[2]);
+    const df var_biased = df_sub(df_div0(s[0], s[2]), df_mul(m, m));
+    const df bias = df_sub(one, df_div0(s[3], df_mul(s[2], s[2])));
+    if (df_ge(s[4], min_weight) && df_pos(bias)) {
+      const df v = df_div0(var_biased, bias);
+      if (OP == kVar) return df_to_f64(v);
+      if (v.hi < 0.0f) return nan;
+      return v.hi == 0.0f ? 0.0 : df_to_f64(df_sqrt(v));
+    }
+    return nan;
+  }
+  if (OP == kCov) {
+    const df cov_biased = df_div0(df_sub(s[2], df_div0(df_mul(s[0], s[1]), s[3])), s[3]);
+    const df bias = df_sub(one, df_div0(s[4], df_mul(s[3], s[3])));
+    return (df_ge(s[5], min_weight) && df_pos(bias)) ? df_to_f64(df_div0(cov_biased, bias)) : nan;
+  }
+  const df cov = df_sub(s[2], df_div0(df_mul(s[0], s[1]), s[3]));
+  const df var1 = df_sub(s[6], df_div0(df_mul(s[0], s[0]), s[3]));
+  const df var2 = df_sub(s[7], df_div0(df_mul(s[1], s[1]), s[3]));
+  const df bias = df_sub(one, df_div0(s[4], df_mul(s[3], s[3])));
+  if (df_ge(s[5], min_weight) && df_pos(bias)) {
+    const df vv = df_mul(var1, var2);
+    if (!df_pos(vv)) return nan;
+    return df_to_f64(df_div0(cov, df_sqrt(vv)));
+  }
+  return nan;
+}
+
 constexpr int NT = 128;
+constexpr int KT = 8;
+constexpr int TILE = NT * KT;
+constexpr int SPAD = TILE + TILE / KT;
+NBG_DEVICE int spad(int p) { return p + p / KT; }
 
 // Phase 0 (PHASE == 0): the map of each tile, composed in position order, to maps[].
 // Phase 2 (PHASE == 2): outputs, starting from the state carries[tile] before the tile.
 // One CTA per tile; tiles do not wait on each other.
-template <int OP, typename T, int K, int PHASE>
+template <int OP, typename T, typename N, int PHASE>
 __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, const T* __restrict__ b,
                                                       const T* __restrict__ alpha_arr, double alpha_scalar,
                                                       int alpha_mode, double min_weight,
                                                       T* __restrict__ out, long long rows, long long n,
-                                                      long long tiles_per_row, Map<Traits<OP>::NS>* maps,
-                                                      const Map<Traits<OP>::NS>* carries) {
+                                                      long long tiles_per_row, Map<Traits<OP>::NS, N>* maps,
+                                                      const Map<Traits<OP>::NS, N>* carries,
+                                                      const double* __restrict__ pivots) {
   constexpr int NS = Traits<OP>::NS;
-  constexpr long long TILE = static_cast<long long>(NT) * K;
-  using M = Map<NS>;
+  constexpr bool TWO = Traits<OP>::TWO;
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  typedef typename BitsOf<T>::type B;
+  typedef typename N::T V;
+  using M = Map<NS, N>;
   __shared__ M warp_tot[NT / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ B sx[SPAD];
+  __shared__ B sy[TWO ? SPAD : 1];
+  __shared__ B sa[SPAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long tile = blockIdx.x;
   const long long row = tile / tiles_per_row;
   const long long chunk = tile - row * tiles_per_row;
-  const long long p0 = chunk * TILE + static_cast<long long>(threadIdx.x) * K;
-  const T* ar = a + row * n;
-  const T* br = Traits<OP>::TWO ? b + row * n : nullptr;
-  const T* alr = alpha_mode == 2 ? alpha_arr + row * n : alpha_arr;
+  const long long t0 = chunk * TILE;
+  const B* ar = as_bits(a) + row * n;
+  const B* br = TWO ? as_bits(b) + row * n : nullptr;
+  const B* alr = alpha_mode == 2 ? as_bits(alpha_arr) + row * n : as_bits(alpha_arr);
+  const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
 
-  T xv[K], yv[K];
-  double al[K];
+  // ---- stage the tile (coalesced), then each thread takes 8 consecutive positions ----
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const long long i = p0 + k;
+  for (int j = 0; j < KT; ++j) {
+    const int p = j * NT + tid;
+    const long long i = t0 + p;
     const bool in = i < n;
-    xv[k] = in ? ar[i] : T(0);
-    yv[k] = (Traits<OP>::TWO && in) ? br[i] : T(0);
-    al[k] = alpha_mode == 0 ? alpha_scalar : (in ? static_cast<double>(alr[i]) : 0.0);
+    sx[spad(p)] = in ? ar[i] : nanb;
+    if (TWO) sy[spad(p)] = in ? br[i] : nanb;
+    if (alpha_mode != 0) sa[spad(p)] = in ? alr[i] : B(0);
   }
+  __syncthreads();
+  V px = N::zero(), py = N::zero();
+  if (SHIFT) {
+    px = as_num(N(), pivots[2 * row]);
+    if (TWO) py = as_num(N(), pivots[2 * row + 1]);
+  }
+  const V al_s = as_num(N(), alpha_scalar);
+  const V d_s = N::sub(N::one(), al_s);
+  const V dd_s = N::mul(d_s, d_s);
+  const int q0 = tid * KT;
+
+  auto position = [&](int k, V& x, V& y, V& al, V& d, V& dd, bool& valid, bool& in) {
+    const int sp = spad(q0 + k);
+    in = t0 + q0 + k < n;
+    const B xb = sx[sp];
+    const B yb = TWO ? sy[sp] : xb;
+    valid = in && !nan_bits(xb) && !(TWO && nan_bits(yb));
+    x = value_as(N(), xb);
+    y = TWO ? value_as(N(), yb) : x;
+    if (SHIFT) {
+      x = N::sub(x, px);
+      if (TWO) y = N::sub(y, py);
+    }
+    if (alpha_mode == 0) {
+      al = al_s;
+      d = d_s;
+      dd = dd_s;
+    } else {
+      al = value_as(N(), sa[sp]);
+      d = N::sub(N::one(), al);
+      dd = N::mul(d, d);
+    }
+  };
+
   // ---- this thread's maps composed in order ----
-  M agg = identity_map<OP>();
+  M agg = identity_map<OP, N>();
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const long long i = p0 + k;
-    if (i >= n) break;
-    const double d = __dadd_rn(1.0, -al[k]);
-    const double dd = __dmul_rn(d, d);
-    bool valid = !is_nan(xv[k]);
-    if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
-    double bj[NS];
-    contributions<OP>(static_cast<double>(xv[k]), static_cast<double>(yv[k]), al[k], bj);
-    agg.A1 = agg.A1 * d;
-    agg.A2 = agg.A2 * dd;
+  for (int k = 0; k < KT; ++k) {
+    V x, y, al, d, dd;
+    bool valid, in;
+    position(k, x, y, al, d, dd, valid, in);
+    if (!in) break;
+    V bj[NS];
+    contributions<OP, N>(x, y, al, bj);
+    agg.A1 = N::mul(agg.A1, d);
+    agg.A2 = N::mul(agg.A2, dd);
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      const double f = (j == Traits<OP>::W2) ? dd : d;
-      agg.B[j] = valid ? fma(agg.B[j], f, bj[j]) : agg.B[j] * f;
+      const V f = (j == Traits<OP>::W2) ? dd : d;
+      agg.B[j] = valid ? N::fma(agg.B[j], f, bj[j]) : N::mul(agg.B[j], f);
     }
     agg.seen |= valid ? 1 : 0;
   }
@@ -214,103 +384,136 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
   M incl = agg;
 #pragma unroll
   for (int dlt = 1; dlt < 32; dlt <<= 1) {
-    const M up = shfl_up_map<OP>(incl, dlt);
-    if (lane >= dlt) incl = compose<OP>(up, incl);
+    const M up = shfl_up_map<OP, N>(incl, dlt);
+    if (lane >= dlt) incl = compose<OP, N>(up, incl);
   }
-  M excl = shfl_up_map<OP>(incl, 1);
-  if (lane == 0) excl = identity_map<OP>();
+  M excl = shfl_up_map<OP, N>(incl, 1);
+  if (lane == 0) excl = identity_map<OP, N>();
   if (lane == 31) warp_tot[warp] = incl;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     M run = warp_tot[0];
     for (int w = 1; w < NT / 32; ++w) {
-      run = compose<OP>(run, warp_tot[w]);
+      run = compose<OP, N>(run, warp_tot[w]);
       warp_tot[w] = run;
     }
   }
   __syncthreads();
   if (PHASE == 0) {
-    if (threadIdx.x == 0) maps[tile] = warp_tot[NT / 32 - 1];
+    if (tid == 0) maps[tile] = warp_tot[NT / 32 - 1];
     return;
   }
-  if (warp > 0) excl = compose<OP>(warp_tot[warp - 1], excl);
+  if (warp > 0) excl = compose<OP, N>(warp_tot[warp - 1], excl);
   // state entering this thread = (excl o carry) applied to the zero state
-  const M start = compose<OP>(carries[tile], excl);
-  double s[NS];
+  const M start = compose<OP, N>(carries[tile], excl);
+  V s[NS];
 #pragma unroll
   for (int j = 0; j < NS; ++j) s[j] = start.B[j];
   int seen = start.seen;
 
-  // ---- the reference's update, position by position ----
-  T* orow = out + row * n;
+  // ---- the reference's update, position by position; outputs back into the stage ----
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const long long i = p0 + k;
-    if (i >= n) break;
-    const double d = __dadd_rn(1.0, -al[k]);
-    const double dd = __dmul_rn(d, d);
+  for (int k = 0; k < KT; ++k) {
+    V x, y, al, d, dd;
+    bool valid, in;
+    position(k, x, y, al, d, dd, valid, in);
+    if (!in) break;
 #pragma unroll
-    for (int j = 0; j < NS; ++j) s[j] = __dmul_rn(s[j], (j == Traits<OP>::W2) ? dd : d);
-    bool valid = !is_nan(xv[k]);
-    if (Traits<OP>::TWO) valid = valid && !is_nan(yv[k]);
+    for (int j = 0; j < NS; ++j) s[j] = N::mul(s[j], (j == Traits<OP>::W2) ? dd : d);
     if (valid) {
-      double bj[NS];
-      contributions<OP>(static_cast<double>(xv[k]), static_cast<double>(yv[k]), al[k], bj);
+      V bj[NS];
+      contributions<OP, N>(x, y, al, bj);
 #pragma unroll
-      for (int j = 0; j < NS; ++j) s[j] = __dadd_rn(s[j], bj[j]);
+      for (int j = 0; j < NS; ++j) s[j] = N::add(s[j], bj[j]);
       seen = 1;
     }
-    orow[i] = static_cast<T>(finalize<OP>(s, seen, min_weight));
+    const T rt = static_cast<T>(finalize<OP>(N(), s, seen, min_weight));
+    sx[spad(q0 + k)] = sizeof(T) == 8 ? static_cast<B>(__double_as_longlong(static_cast<double>(rt)))
+                                      : static_cast<B>(__float_as_uint(static_cast<float>(rt)));
+  }
+  __syncthreads();
+  B* ob = as_bits(out) + row * n;
+#pragma unroll
+  for (int j = 0; j < KT; ++j) {
+    const int p = j * NT + tid;
+    if (t0 + p < n) ob[t0 + p] = sx[spad(p)];
   }
 }
 
 // Phase 1: per row, the state before each tile, composing the tile maps in a fixed
 // order (a block-wide scan over chunks of NT tiles), so the carries are reproducible.
-template <int OP>
-__global__ void __launch_bounds__(NT) exp_carry_kernel(const Map<Traits<OP>::NS>* __restrict__ maps,
-                                                       Map<Traits<OP>::NS>* __restrict__ carries,
+template <int OP, typename N>
+__global__ void __launch_bounds__(NT) exp_carry_kernel(const Map<Traits<OP>::NS, N>* __restrict__ maps,
+                                                       Map<Traits<OP>::NS, N>* __restrict__ carries,
                                                        long long tiles_per_row) {
-  using M = Map<Traits<OP>::NS>;
+  using M = Map<Traits<OP>::NS, N>;
   __shared__ M warp_tot[NT / 32];
   __shared__ M running_smem;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long row = blockIdx.x;
   const M* mr = maps + row * tiles_per_row;
   M* cr = carries + row * tiles_per_row;
-  if (threadIdx.x == 0) running_smem = identity_map<OP>();
+  if (threadIdx.x == 0) running_smem = identity_map<OP, N>();
   __syncthreads();
   for (long long base = 0; base < tiles_per_row; base += NT) {
     const long long t = base + threadIdx.x;
-    M v = t < tiles_per_row ? mr[t] : identity_map<OP>();
+    M v = t < tiles_per_row ? mr[t] : identity_map<OP, N>();
     M incl = v;
 #pragma unroll
     for (int dlt = 1; dlt < 32; dlt <<= 1) {
-      const M up = shfl_up_map<OP>(incl, dlt);
-      if (lane >= dlt) incl = compose<OP>(up, incl);
+      const M up = shfl_up_map<OP, N>(incl, dlt);
+      if (lane >= dlt) incl = compose<OP, N>(up, incl);
     }
-    M excl = shfl_up_map<OP>(incl, 1);
-    if (lane == 0) excl = identity_map<OP>();
+    M excl = shfl_up_map<OP, N>(incl, 1);
+    if (lane == 0) excl = identity_map<OP, N>();
     if (lane == 31) warp_tot[warp] = incl;
     __syncthreads();
     if (threadIdx.x == 0) {
       M run = warp_tot[0];
       for (int w = 1; w < NT / 32; ++w) {
-        run = compose<OP>(run, warp_tot[w]);
+        run = compose<OP, N>(run, warp_tot[w]);
         warp_tot[w] = run;
       }
     }
     __syncthreads();
-    if (warp > 0) excl = compose<OP>(warp_tot[warp - 1], excl);
+    if (warp > 0) excl = compose<OP, N>(warp_tot[warp - 1], excl);
     const M running = running_smem;
     if (t < tiles_per_row) {
-      M c = compose<OP>(running, excl);
-      c.A1 = 0.0;  // only the state (B) is used downstream
-      c.A2 = 0.0;
+      M c = compose<OP, N>(running, excl);
+      c.A1 = N::zero();  // only the state (B) is used downstream
+      c.A2 = N::zero();
       cr[t] = c;
     }
     __syncthreads();
-    if (threadIdx.x == 0) running_smem = compose<OP>(running, warp_tot[NT / 32 - 1]);
+    if (threadIdx.x == 0) running_smem = compose<OP, N>(running, warp_tot[NT / 32 - 1]);
     __syncthreads();
+  }
+}
+
+// The pivot of each row (and of b): its first finite value, 0 if none.  One warp per row.
+template <typename T>
+__global__ void exp_pivot_kernel(const T* __restrict__ a, const T* __restrict__ b, long long rows, long long n,
+                                 double* __restrict__ pivots) {
+  typedef typename BitsOf<T>::type B;
+  const int lane = threadIdx.x & 31;
+  const long long row = static_cast<long long>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (row >= rows) return;
+  for (int which = 0; which < (b ? 2 : 1); ++which) {
+    const B* r = as_bits(which ? b : a) + row * n;
+    double p = 0.0;
+    for (long long base = 0; base < n; base += 32) {
+      const long long i = base + lane;
+      const B v = i < n ? r[i] : B(0);
+      const bool ok = i < n && !nan_bits(v) && ((sizeof(B) == 8) ? ((static_cast<unsigned long long>(v) >> 52 & 0x7ff) != 0x7ff)
+                                                                 : ((static_cast<unsigned>(v) >> 23 & 0xff) != 0xff));
+      const unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (m) {
+        const B f = __shfl_sync(0xffffffffu, v, __ffs(m) - 1);
+        p = sizeof(B) == 8 ? __longlong_as_double(static_cast<long long>(f)) : static_cast<double>(__int_as_float(static_cast<int>(f)));
+        break;
+      }
+    }
+    if (lane == 0) pivots[2 * row + which] = p;
   }
 }
 
@@ -321,19 +524,16 @@ using namespace nbg;
 using namespace nbg::mexp;
 
 namespace {
-constexpr int kExpK = 8;
 
-long long exp_tiles_per_row(long long n) {
-  const long long tile = static_cast<long long>(NT) * kExpK;
-  return n <= 0 ? 0 : (n + tile - 1) / tile;
-}
+long long exp_tiles_per_row(long long n) { return n <= 0 ? 0 : (n + TILE - 1) / TILE; }
 
 template <int OP>
 size_t exp_scratch_bytes(long long rows, long long n) {
-  return 2 * static_cast<size_t>(rows * exp_tiles_per_row(n)) * sizeof(Map<Traits<OP>::NS>) + 256;
+  return 2 * static_cast<size_t>(rows * exp_tiles_per_row(n)) * sizeof(Map<Traits<OP>::NS, F64>) + 512 +
+         static_cast<size_t>(rows) * 16;
 }
 
-template <int OP, typename T>
+template <int OP, typename T, typename N>
 int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int alpha_mode,
                double min_weight, T* out, long long rows, long long n, void* ws, size_t ws_bytes,
                cudaStream_t s) {
@@ -344,16 +544,25 @@ int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int 
   const long long total = rows * tpr;
   if (total > 0x7fffffffll) return kUnsupported;
   if (!ws || ws_bytes < exp_scratch_bytes<OP>(rows, n)) return kWorkspaceTooSmall;
-  using M = Map<Traits<OP>::NS>;
+  using M = Map<Traits<OP>::NS, N>;
+  static_assert(sizeof(M) == sizeof(Map<Traits<OP>::NS, F64>), "both policies use 8-byte numbers");
   M* maps = reinterpret_cast<M*>((reinterpret_cast<size_t>(ws) + 127) & ~static_cast<size_t>(127));
   M* carries = maps + total;
+  double* pivots = reinterpret_cast<double*>((reinterpret_cast<size_t>(carries + total) + 127) & ~static_cast<size_t>(127));
+  int launches = 3;
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  if (SHIFT) {
+    exp_pivot_kernel<T><<<static_cast<int>((rows + 7) / 8), 256, 0, s>>>(a, Traits<OP>::TWO ? b : nullptr, rows, n,
+                                                                        pivots);
+    ++launches;
+  }
   const int grid = static_cast<int>(total);
-  exp_tile_kernel<OP, T, kExpK, 0><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight,
-                                                       out, rows, n, tpr, maps, carries);
-  exp_carry_kernel<OP><<<static_cast<int>(rows), NT, 0, s>>>(maps, carries, tpr);
-  exp_tile_kernel<OP, T, kExpK, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight,
-                                                       out, rows, n, tpr, maps, carries);
-  note_launches(3);
+  exp_tile_kernel<OP, T, N, 0><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n,
+                                                   tpr, maps, carries, pivots);
+  exp_carry_kernel<OP, N><<<static_cast<int>(rows), NT, 0, s>>>(maps, carries, tpr);
+  exp_tile_kernel<OP, T, N, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n,
+                                                   tpr, maps, carries, pivots);
+  note_launches(launches);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 }  // namespace
@@ -367,34 +576,42 @@ size_t nbg_move_exp_workspace_bytes(long long rows, long long n) {
 
 // alpha_mode: 0 = scalar `alpha_scalar`, 1 = `alpha` has n values shared by all rows,
 // 2 = `alpha` has rows*n values laid out like `a`.
-#define NBG_EXP1(NAME, OPC, T, SFX)                                                            \
-  int nbg_##NAME##_##SFX(const T* a, const T* alpha, double alpha_scalar, int alpha_mode,       \
-                         double min_weight, T* out, long long rows, long long n, void* ws,      \
-                         size_t ws_bytes, void* stream) {                                       \
-    return launch_exp<OPC, T>(a, nullptr, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, \
-                              n, ws, ws_bytes, static_cast<cudaStream_t>(stream));             \
+#define NBG_EXP1(NAME, OPC, T, SFX, N)                                                           \
+  int nbg_##NAME##_##SFX(const T* a, const T* alpha, double alpha_scalar, int alpha_mode,         \
+                         double min_weight, T* out, long long rows, long long n, void* ws,        \
+                         size_t ws_bytes, void* stream) {                                         \
+    return launch_exp<OPC, T, N>(a, nullptr, alpha, alpha_scalar, alpha_mode, min_weight, out,   \
+                                 rows, n, ws, ws_bytes, static_cast<cudaStream_t>(stream));      \
   }
-#define NBG_EXP2(NAME, OPC, T, SFX)                                                            \
-  int nbg_##NAME##_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,           \
-                         int alpha_mode, double min_weight, T* out, long long rows, long long n, \
-                         void* ws, size_t ws_bytes, void* stream) {                             \
-    return launch_exp<OPC, T>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n,   \
-                              ws, ws_bytes, static_cast<cudaStream_t>(stream));                \
+#define NBG_EXP2(NAME, OPC, T, SFX, N)                                                           \
+  int nbg_##NAME##_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,             \
+                         int alpha_mode, double min_weight, T* out, long long rows, long long n,   \
+                         void* ws, size_t ws_bytes, void* stream) {                               \
+    return launch_exp<OPC, T, N>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n, \
+                                 ws, ws_bytes, static_cast<cudaStream_t>(stream));               \
   }
 
-NBG_EXP1(move_exp_nancount, kCount, double, f64)
-NBG_EXP1(move_exp_nancount, kCount, float, f32)
-NBG_EXP1(move_exp_nanmean, kMean, double, f64)
-NBG_EXP1(move_exp_nanmean, kMean, float, f32)
-NBG_EXP1(move_exp_nansum, kSum, double, f64)
-NBG_EXP1(move_exp_nansum, kSum, float, f32)
-NBG_EXP1(move_exp_nanvar, kVar, double, f64)
-NBG_EXP1(move_exp_nanvar, kVar, float, f32)
-NBG_EXP1(move_exp_nanstd, kStd, double, f64)
-NBG_EXP1(move_exp_nanstd, kStd, float, f32)
-NBG_EXP2(move_exp_nancov, kCov, double, f64)
-NBG_EXP2(move_exp_nancov, kCov, float, f32)
-NBG_EXP2(move_exp_nancorr, kCorr, double, f64)
-NBG_EXP2(move_exp_nancorr, kCorr, float, f32)
+NBG_EXP1(move_exp_nancount, kCount, double, f64, F64)
+NBG_EXP1(move_exp_nancount, kCount, float, f32, F64)
+NBG_EXP1(move_exp_nanmean, kMean, double, f64, F64)
+NBG_EXP1(move_exp_nanmean, kMean, float, f32, F64)
+NBG_EXP1(move_exp_nansum, kSum, double, f64, F64)
+NBG_EXP1(move_exp_nansum, kSum, float, f32, F64)
+NBG_EXP1(move_exp_nanvar, kVar, double, f64, F64)
+NBG_EXP1(move_exp_nanvar, kVar, float, f32, F64)
+NBG_EXP1(move_exp_nanstd, kStd, double, f64, F64)
+NBG_EXP1(move_exp_nanstd, kStd, float, f32, F64)
+NBG_EXP2(move_exp_nancov, kCov, double, f64, F64)
+NBG_EXP2(move_exp_nancov, kCov, float, f32, F64)
+NBG_EXP2(move_exp_nancorr, kCorr, double, f64, F64)
+NBG_EXP2(move_exp_nancorr, kCorr, float, f32, F64)
+// FP32-compensated forms of the float64 entry points (double-float on the FP32 pipes)
+NBG_EXP1(move_exp_nancount, kCount, double, f64_fp32c, DF)
+NBG_EXP1(move_exp_nanmean, kMean, double, f64_fp32c, DF)
+NBG_EXP1(move_exp_nansum, kSum, double, f64_fp32c, DF)
+NBG_EXP1(move_exp_nanvar, kVar, double, f64_fp32c, DF)
+NBG_EXP1(move_exp_nanstd, kStd, double, f64_fp32c, DF)
+NBG_EXP2(move_exp_nancov, kCov, double, f64_fp32c, DF)
+NBG_EXP2(move_exp_nancorr, kCorr, double, f64_fp32c, DF)
 
 }  // extern "C"

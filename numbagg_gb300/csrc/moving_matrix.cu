@@ -66,14 +66,23 @@ NBG_DEVICE float finish(float si, float sj, float pr, float qi, float qj, long l
     const float rn = nn < kRcp ? rcp[nn] : 1.0f / static_cast<float>(nn);
     const float rm = nn - 1 < kRcp ? rcp[nn - 1] : 1.0f / static_cast<float>(nn - 1);
     const float mi = si * rn, mj = sj * rn;
-    return (pr * rn - mi * mj) * (static_cast<float>(nn) * rm);
+    const float p = __fmul_rn(mi, mj);  // subtracted exactly, as in the correlation below
+    const float c = __fsub_rn(__fmaf_rn(pr, rn, -p), __fmaf_rn(mi, mj, -p));
+    return c * (static_cast<float>(nn) * rm);
   }
   if (nn < (mc > 2 ? mc : 2)) return nan;
   const float rn = nn < kRcp ? rcp[nn] : 1.0f / static_cast<float>(nn);
   const float mi = si * rn, mj = sj * rn;
-  const float vi = qi * rn - mi * mi;
-  const float vj = qj * rn - mj * mj;
-  const float cv = pr * rn - mi * mj;
+  // q * rn - m * m with the product subtracted exactly (its rounding error recovered by
+  // an FMA), so the cancellation at small counts costs no extra digits
+  auto diff = [](float q, float r, float x, float y) {
+    const float p = __fmul_rn(x, y);
+    const float e = __fmaf_rn(x, y, -p);
+    return __fsub_rn(__fmaf_rn(q, r, -p), e);
+  };
+  const float vi = diff(qi, rn, mi, mi);
+  const float vj = diff(qj, rn, mj, mj);
+  const float cv = diff(pr, rn, mi, mj);
   return (vi > 0.0f && vj > 0.0f) ? cv * rsqrtf(vi * vj) : nan;
 }
 

@@ -20,7 +20,12 @@ import torch
 from . import _host, _lib
 
 
-def _move(name: str, arrs, window, min_count, axis):
+PRECISIONS = ("f64", "fp32c")
+
+
+def _move(name: str, arrs, window, min_count, axis, precision="f64"):
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}: {precision!r}")
     if min_count is None:
         min_count = window
     elif min_count < 0:
@@ -64,7 +69,10 @@ def _move(name: str, arrs, window, min_count, axis):
     if out.numel():
         L = _lib.lib()
         ws = _lib.workspaces.scratch(L.nbg_move_workspace_bytes(rows, n), a.device)
-        fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
+        sfx = _host.FLOAT_SFX[dtype]
+        if precision == "fp32c" and dtype == torch.float64:
+            sfx += "_fp32c"
+        fn = getattr(L, f"nbg_{name}_{sfx}")
         args = [f.data_ptr() for f in flats] + [
             out.data_ptr(),
             rows,
@@ -79,34 +87,34 @@ def _move(name: str, arrs, window, min_count, axis):
     return restore(_host.restore_axis(out, shape, axis))
 
 
-def move_sum(arr, /, *, window, min_count=None, axis=-1):
+def move_sum(arr, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving sum over the last `window` values, skipping NaN (numbagg/moving.py:58-99)."""
-    return _move("move_sum", (arr,), window, min_count, axis)
+    return _move("move_sum", (arr,), window, min_count, axis, precision)
 
 
-def move_mean(arr, /, *, window, min_count=None, axis=-1):
+def move_mean(arr, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving mean over the last `window` values, skipping NaN (numbagg/moving.py:12-55)."""
-    return _move("move_mean", (arr,), window, min_count, axis)
+    return _move("move_mean", (arr,), window, min_count, axis, precision)
 
 
-def move_std(arr, /, *, window, min_count=None, axis=-1):
+def move_std(arr, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving sample standard deviation (ddof=1) (numbagg/moving.py:123-151)."""
-    return _move("move_std", (arr,), window, min_count, axis)
+    return _move("move_std", (arr,), window, min_count, axis, precision)
 
 
-def move_var(arr, /, *, window, min_count=None, axis=-1):
+def move_var(arr, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving sample variance (ddof=1) (numbagg/moving.py:154-181)."""
-    return _move("move_var", (arr,), window, min_count, axis)
+    return _move("move_var", (arr,), window, min_count, axis, precision)
 
 
-def move_cov(a, b, /, *, window, min_count=None, axis=-1):
+def move_cov(a, b, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving sample covariance of pairwise-complete values (numbagg/moving.py:184-220)."""
-    return _move("move_cov", (a, b), window, min_count, axis)
+    return _move("move_cov", (a, b), window, min_count, axis, precision)
 
 
-def move_corr(a, b, /, *, window, min_count=None, axis=-1):
+def move_corr(a, b, /, *, window, min_count=None, axis=-1, precision="f64"):
     """Moving correlation of pairwise-complete values (numbagg/moving.py:223-275)."""
-    return _move("move_corr", (a, b), window, min_count, axis)
+    return _move("move_corr", (a, b), window, min_count, axis, precision)
 
 
 __all__ = ["move_corr", "move_cov", "move_mean", "move_std", "move_sum", "move_var"]

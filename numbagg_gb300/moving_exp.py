@@ -15,7 +15,12 @@ import torch
 from . import _host, _lib
 
 
-def _move_exp(name: str, arrs, alpha, min_weight, axis):
+PRECISIONS = ("f64", "fp32c")
+
+
+def _move_exp(name: str, arrs, alpha, min_weight, axis, precision="f64"):
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}: {precision!r}")
     if isinstance(axis, tuple):
         if axis == ():
             if len(arrs) > 1:
@@ -74,7 +79,10 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis):
     if out.numel():
         L = _lib.lib()
         ws = _lib.workspaces.scratch(L.nbg_move_exp_workspace_bytes(rows, n), a.device)
-        fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
+        sfx = _host.FLOAT_SFX[dtype]
+        if precision == "fp32c" and dtype == torch.float64:
+            sfx += "_fp32c"
+        fn = getattr(L, f"nbg_{name}_{sfx}")
         args = [f.data_ptr() for f in flats] + [
             None if alpha_t is None else alpha_t.data_ptr(),
             alpha_scalar,
@@ -91,39 +99,39 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis):
     return restore(_host.restore_axis(out, shape, axis))
 
 
-def move_exp_nancount(arr, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nancount(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially decayed count of non-NaN values (numbagg/moving_exp.py:12-38)."""
-    return _move_exp("move_exp_nancount", (arr,), alpha, min_weight, axis)
+    return _move_exp("move_exp_nancount", (arr,), alpha, min_weight, axis, precision)
 
 
-def move_exp_nanmean(arr, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nanmean(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving mean (numbagg/moving_exp.py:41-71)."""
-    return _move_exp("move_exp_nanmean", (arr,), alpha, min_weight, axis)
+    return _move_exp("move_exp_nanmean", (arr,), alpha, min_weight, axis, precision)
 
 
-def move_exp_nansum(arr, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nansum(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving sum (numbagg/moving_exp.py:74-102)."""
-    return _move_exp("move_exp_nansum", (arr,), alpha, min_weight, axis)
+    return _move_exp("move_exp_nansum", (arr,), alpha, min_weight, axis, precision)
 
 
-def move_exp_nanvar(arr, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nanvar(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving variance, bias-corrected (numbagg/moving_exp.py:105-156)."""
-    return _move_exp("move_exp_nanvar", (arr,), alpha, min_weight, axis)
+    return _move_exp("move_exp_nanvar", (arr,), alpha, min_weight, axis, precision)
 
 
-def move_exp_nanstd(arr, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nanstd(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving standard deviation (numbagg/moving_exp.py:158-223)."""
-    return _move_exp("move_exp_nanstd", (arr,), alpha, min_weight, axis)
+    return _move_exp("move_exp_nanstd", (arr,), alpha, min_weight, axis, precision)
 
 
-def move_exp_nancov(a1, a2, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nancov(a1, a2, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving covariance (numbagg/moving_exp.py:226-272)."""
-    return _move_exp("move_exp_nancov", (a1, a2), alpha, min_weight, axis)
+    return _move_exp("move_exp_nancov", (a1, a2), alpha, min_weight, axis, precision)
 
 
-def move_exp_nancorr(a1, a2, /, *, alpha, min_weight=0, axis=-1):
+def move_exp_nancorr(a1, a2, /, *, alpha, min_weight=0, axis=-1, precision="f64"):
     """Exponentially weighted moving correlation (numbagg/moving_exp.py:275-335)."""
-    return _move_exp("move_exp_nancorr", (a1, a2), alpha, min_weight, axis)
+    return _move_exp("move_exp_nancorr", (a1, a2), alpha, min_weight, axis, precision)
 
 
 __all__ = [

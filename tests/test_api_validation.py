@@ -111,3 +111,18 @@ def test_public_names_match_numbagg_hot_path():
         "group_nanprod", "group_nanstd", "group_nansum", "group_nansum_of_squares", "group_nanvar",
     }
     assert expected <= set(nb.__all__)
+
+
+@pytest.mark.parametrize(
+    "call",
+    [
+        lambda x: nb.move_mean(x, window=3, precision="fp16"),
+        lambda x: nb.move_corr(x, x, window=3, precision="bf16"),
+        lambda x: nb.move_exp_nanvar(x, alpha=0.5, precision="double"),
+    ],
+)
+def test_precision_keyword_checked_before_device_work(call):
+    # precision= is this package's extension ("f64" default, or "fp32c"); a bad value
+    # raises on the host, so no GPU is needed to see it
+    with pytest.raises(ValueError, match="precision"):
+        call(np.zeros((2, 10)))
