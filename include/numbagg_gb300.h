@@ -98,6 +98,25 @@ NBG_DECL_MOVE1(move_std, double, f64_fp32c)
 NBG_DECL_MOVE2(move_cov, double, f64_fp32c)
 NBG_DECL_MOVE2(move_corr, double, f64_fp32c)
 
+/* Ragged batches of moving windows (no reference counterpart: numbagg applies its
+ * functions array by array; these run many series of uneven length in one call).
+ * values: the series back to back, series s = values[offsets[s] : offsets[s + 1]];
+ * offsets: nseries + 1 device int64, offsets[0] = 0, nondecreasing; out: like values.
+ * ws: nbg_move_workspace_bytes(nseries, 0) bytes of scratch; chunk_len: positions per
+ * work item (0 = default: eight windows, at least 32768). */
+#define NBG_DECL_MOVE_RAGGED(NAME, SFX)                                                          \
+  NBG_API int nbg_##NAME##_ragged_##SFX(const double* values, const long long* offsets, long long nseries, \
+                                        double* out, long long window, long long min_count,             \
+                                        long long chunk_len, void* ws, size_t ws_bytes, void* stream);
+NBG_DECL_MOVE_RAGGED(move_sum, f64)
+NBG_DECL_MOVE_RAGGED(move_mean, f64)
+NBG_DECL_MOVE_RAGGED(move_var, f64)
+NBG_DECL_MOVE_RAGGED(move_std, f64)
+NBG_DECL_MOVE_RAGGED(move_sum, f64_fp32c)
+NBG_DECL_MOVE_RAGGED(move_mean, f64_fp32c)
+NBG_DECL_MOVE_RAGGED(move_var, f64_fp32c)
+NBG_DECL_MOVE_RAGGED(move_std, f64_fp32c)
+
 /* ---- exponentially weighted moving functions ---------------------------------------
  * Replaces the gufuncs built by ndmoveexp (numbagg/decorators.py:344-414) from
  *   move_exp_nancount numbagg/moving_exp.py:12-38    move_exp_nanmean numbagg/moving_exp.py:41-71
@@ -142,6 +161,23 @@ NBG_DECL_EXP1(move_exp_nanvar, double, f64_fp32c)
 NBG_DECL_EXP1(move_exp_nanstd, double, f64_fp32c)
 NBG_DECL_EXP2(move_exp_nancov, double, f64_fp32c)
 NBG_DECL_EXP2(move_exp_nancorr, double, f64_fp32c)
+
+/* Ragged batches of exponentially weighted functions (no reference counterpart):
+ * series as for the moving windows, `total` = offsets[nseries]; alpha_mode 0 (scalar
+ * alpha_scalar) or 2 (one alpha per value, laid out like values).  ws:
+ * nbg_move_exp_ragged_workspace_bytes(nseries, total) bytes of scratch. */
+NBG_API size_t nbg_move_exp_ragged_workspace_bytes(long long nseries, long long total);
+#define NBG_DECL_EXP_RAGGED(NAME, SFX)                                                              \
+  NBG_API int nbg_##NAME##_ragged_##SFX(const double* values, const long long* offsets, long long nseries, \
+                                        long long total, const double* alpha, double alpha_scalar,      \
+                                        int alpha_mode, double min_weight, double* out, void* ws,       \
+                                        size_t ws_bytes, void* stream);
+NBG_DECL_EXP_RAGGED(move_exp_nanmean, f64)
+NBG_DECL_EXP_RAGGED(move_exp_nanvar, f64)
+NBG_DECL_EXP_RAGGED(move_exp_nanstd, f64)
+NBG_DECL_EXP_RAGGED(move_exp_nanmean, f64_fp32c)
+NBG_DECL_EXP_RAGGED(move_exp_nanvar, f64_fp32c)
+NBG_DECL_EXP_RAGGED(move_exp_nanstd, f64_fp32c)
 
 /* ---- fills --------------------------------------------------------------------------
  * Replaces the gufuncs built by ndfill (numbagg/decorators.py:417-487) from
@@ -211,6 +247,22 @@ NBG_DECL_GROUP_ALL(nanlast)           /* numbagg/grouped.py:113-121 */
 NBG_DECL_GROUP_ALL(nanprod)           /* numbagg/grouped.py:124-132 */
 NBG_DECL_GROUP_ALL(nanany)            /* numbagg/grouped.py:247-257 */
 NBG_DECL_GROUP_ALL(nanall)            /* numbagg/grouped.py:260-270 */
+
+/* Ragged batches of labelled reductions (no reference counterpart): values and labels
+ * flat (`total` values), series s = [offsets[s], offsets[s + 1]) with its own labels;
+ * out: nseries x num_labels float64 (num_labels <= 8192).  Deterministic: per-chunk
+ * partials folded in chunk order.  ws: nbg_group_ragged_workspace_bytes() bytes. */
+NBG_API size_t nbg_group_ragged_workspace_bytes(long long nseries, long long total, long long num_labels);
+#define NBG_DECL_GROUP_RAGGED(NAME, L, LS)                                                                 \
+  NBG_API int nbg_group_##NAME##_ragged_f64_##LS(const double* values, const L* labels, const long long* offsets, \
+                                                 long long nseries, long long total, long long num_labels,     \
+                                                 double* out, void* ws, size_t ws_bytes, void* stream);
+NBG_DECL_GROUP_RAGGED(nansum, int, i32)
+NBG_DECL_GROUP_RAGGED(nansum, long long, i64)
+NBG_DECL_GROUP_RAGGED(nanmean, int, i32)
+NBG_DECL_GROUP_RAGGED(nanmean, long long, i64)
+NBG_DECL_GROUP_RAGGED(nancount, int, i32)
+NBG_DECL_GROUP_RAGGED(nancount, long long, i64)
 
 /* ---- moving covariance / correlation matrices ----------------------------------------
  * Replaces the gufuncs built by ndmovematrix (numbagg/decorators.py:747-818) from

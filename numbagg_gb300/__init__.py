@@ -36,6 +36,7 @@ from .moving_exp import (
     move_exp_nanvar,
 )
 from .moving_matrix import move_corrmatrix, move_covmatrix
+from . import ragged  # noqa: E402  (ragged batches: an extension)
 
 __version__ = "1.0.0"
 

@@ -85,6 +85,17 @@ def _declare(lib: ctypes.CDLL) -> None:
         sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
     for f in ("move_exp_nancov", "move_exp_nancorr"):
         sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
+    # ragged batches
+    sig("nbg_move_exp_ragged_workspace_bytes", c_sz, c_ll, c_ll)
+    sig("nbg_group_ragged_workspace_bytes", c_sz, c_ll, c_ll, c_ll)
+    for sfx in ("f64", "f64_fp32c"):
+        for f in ("move_sum", "move_mean", "move_var", "move_std"):
+            sig(f"nbg_{f}_ragged_{sfx}", c_i, c_vp, c_vp, c_ll, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+        for f in ("move_exp_nanmean", "move_exp_nanvar", "move_exp_nanstd"):
+            sig(f"nbg_{f}_ragged_{sfx}", c_i, c_vp, c_vp, c_ll, c_ll, c_vp, c_d, c_i, c_d, c_vp, c_vp, c_sz, c_vp)
+    for f in ("nansum", "nanmean", "nancount"):
+        for ls in ("i32", "i64"):
+            sig(f"nbg_group_{f}_ragged_f64_{ls}", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_vp, c_sz, c_vp)
     for dt in ("f64", "f32", "i32", "i64"):
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)

@@ -83,3 +83,55 @@ extern "C" int nbg_debug_lookback_timeout(void* ws, size_t ws_bytes, int spin_li
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
+
+namespace nbg {
+__global__ void ragged_plan_kernel(const long long* __restrict__ offsets, long long rows, long long item_len,
+                                   long long* __restrict__ item_start) {
+  __shared__ long long warp_sum[32];
+  __shared__ long long carry;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (long long base = 0; base < rows; base += blockDim.x) {
+    const long long s = base + tid;
+    long long v = 0;
+    if (s < rows) {
+      const long long len = offsets[s + 1] - offsets[s];
+      v = len > 0 ? (len + item_len - 1) / item_len : 0;
+    }
+    long long incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const long long up = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += up;
+    }
+    if (lane == 31) warp_sum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const int nw = blockDim.x / 32;
+      long long w = lane < nw ? warp_sum[lane] : 0;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const long long up = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= d) w += up;
+      }
+      if (lane < nw) warp_sum[lane] = w;
+    }
+    __syncthreads();
+    const long long excl = carry + (warp ? warp_sum[warp - 1] : 0) + incl - v;
+    if (s < rows) item_start[s] = excl;
+    __syncthreads();
+    if (tid == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (tid == 0) item_start[rows] = carry;
+}
+
+int layout_grid(long long max_items, int per_sm) {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long cap = static_cast<long long>(sms) * per_sm;
+  return static_cast<int>(max_items < cap ? (max_items > 0 ? max_items : 1) : cap);
+}
+}  // namespace nbg

@@ -892,6 +892,102 @@ __global__ void fold_mom_kernel(const MomPart* __restrict__ parts, O* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------------
+// ragged series with their own labels (values and labels flat, series s covering
+// [offsets[s], offsets[s + 1])): chunks of kRagCols values, CTA-shared fixed-point bins
+// at the chunk's largest exponent, one partial per chunk and label, folded per series
+// in chunk order (deterministic).
+// ---------------------------------------------------------------------------------
+constexpr int kRagCols = FT * 16;
+
+template <int F, typename L>
+__global__ void __launch_bounds__(FT) ragged_mom_kernel(const double* __restrict__ values,
+                                                        const L* __restrict__ labels, Layout lay, int K,
+                                                        MomPart* __restrict__ parts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* b1 = reinterpret_cast<unsigned long long*>(smem_raw);  // [K]
+  unsigned* cnt = reinterpret_cast<unsigned*>(b1 + K);                       // [K]
+  unsigned* infc = cnt + K;                                                   // [K]: +1 per +inf, +65536 per -inf
+  __shared__ int red[FT / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long items = layout_items(lay);
+  for (long long id = blockIdx.x; id < items; id += gridDim.x) {
+    const Item it = layout_item(lay, id);
+    const long long c0 = it.index * kRagCols, c1 = min(it.len, c0 + kRagCols);
+    for (int k = tid; k < K; k += FT) {
+      b1[k] = 0;
+      cnt[k] = 0;
+      infc[k] = 0;
+    }
+    unsigned long long v[16];
+    int lab[16];
+    int emax = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const long long col = c0 + j * FT + tid;
+      const bool in = col < c1;
+      v[j] = in ? __ldcs(reinterpret_cast<const unsigned long long*>(values) + it.base + col) : 0ull;
+      const long long l = in ? static_cast<long long>(__ldg(labels + it.base + col)) : -1;
+      lab[j] = (l >= 0 && l < K && !nan_bits(v[j])) ? static_cast<int>(l) : -1;
+      const Dec d = decomp(v[j]);
+      if (lab[j] >= 0 && !d.special) emax = max(emax, d.e);
+    }
+    emax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
+    if (lane == 0) red[warp] = emax;
+    __syncthreads();  // also orders the bin reset before the updates
+    int E = 1;
+#pragma unroll
+    for (int w = 0; w < FT / 32; ++w) E = max(E, red[w]);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (lab[j] < 0) continue;
+      atomicAdd(&cnt[lab[j]], 1u);
+      const Dec d = decomp(v[j]);
+      if (d.special) {
+        atomicAdd(&infc[lab[j]], d.neg ? 65536u : 1u);
+        continue;
+      }
+      if (Need<F>::s1) {
+        const int sh = E - d.e + 4;  // 49-bit terms: 4096 of them fit in 63 bits
+        const unsigned long long a = sh >= 64 ? 0ull : (d.m >> sh);
+        atomicAdd(&b1[lab[j]], d.neg ? (~a + 1ull) : a);
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < K; k += FT) {
+      MomPart p;
+      p.s1 = Need<F>::s1 ? fx::to_f64(static_cast<fx::i128>(static_cast<long long>(b1[k])), E + 4 - 1075) : 0.0;
+      p.s2 = 0.0;
+      p.cnt = cnt[k];
+      p.pinf = static_cast<int>(infc[k] & 0xffffu);
+      p.ninf = static_cast<int>(infc[k] >> 16);
+      parts[id * K + k] = p;
+    }
+    __syncthreads();
+  }
+}
+
+template <int F>
+__global__ void ragged_fold_kernel(const MomPart* __restrict__ parts, double* __restrict__ out, Layout lay,
+                                   long long K) {
+  const long long total = lay.rows * K;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const long long s = t / K, k = t - s * K;
+    double s1 = 0.0;
+    long long c = 0;
+    int pinf = 0, ninf = 0;
+    for (long long id = lay.item_start[s]; id < lay.item_start[s + 1]; ++id) {
+      const MomPart p = parts[id * K + k];
+      s1 += p.s1;
+      c += p.cnt;
+      pinf += p.pinf;
+      ninf += p.ninf;
+    }
+    out[t] = finish_mom<F, double>(s1, 0.0, c, pinf, ninf, 1);
+  }
+}
+
 // accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]
 template <int F, typename O, int RB>
 __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
@@ -1210,6 +1306,33 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 
+inline size_t ragged_group_bytes(long long nseries, long long total, long long K) {
+  return static_cast<size_t>(total / kRagCols + nseries) * static_cast<size_t>(K) * sizeof(MomPart) +
+         static_cast<size_t>(nseries + 1) * 8 + 1024;
+}
+
+template <int F, typename L>
+int launch_ragged_group(const double* values, const L* labels, const long long* offsets, long long nseries,
+                        long long total, long long K, double* out, void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (nseries < 0 || total < 0 || K < 0) return kInvalidArgument;
+  if (nseries == 0 || K == 0) return kOk;
+  if (!offsets || !out || (total > 0 && (!values || !labels))) return kInvalidArgument;
+  if (K > 8192) return kUnsupported;
+  if (!ws || ws_bytes < ragged_group_bytes(nseries, total, K)) return kWorkspaceTooSmall;
+  unsigned char* cur = static_cast<unsigned char*>(ws);
+  MomPart* parts = carve<MomPart>(cur, (total / kRagCols + nseries) * K);
+  long long* item_start = carve<long long>(cur, nseries + 1);
+  Layout lay{offsets, item_start, nseries, 0, 0};
+  ragged_plan_kernel<<<1, 1024, 0, s>>>(offsets, nseries, kRagCols, item_start);
+  const size_t smem = static_cast<size_t>(K) * 16;
+  auto kern = ragged_mom_kernel<F, L>;
+  set_smem(kern, smem);
+  kern<<<layout_grid(LLONG_MAX, 4), FT, smem, s>>>(values, labels, lay, static_cast<int>(K), parts);
+  ragged_fold_kernel<F><<<fin_grid(nseries * K), 256, 0, s>>>(parts, out, lay, K);
+  note_launches(3);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
+
 }  // namespace grouped
 }  // namespace nbg
 
@@ -1271,4 +1394,23 @@ NBG_GFAST_ALL(nanmax, kMax)
 NBG_GFAST_ALL(nanmin, kMin)
 NBG_GFAST_ALL(nanfirst, kFirst)
 NBG_GFAST_ALL(nanlast, kLast)
+
+// Ragged series with their own labels: values, labels: `total` values in series
+// s = [offsets[s], offsets[s + 1]); out: nseries x num_labels (float64).
+size_t nbg_group_ragged_workspace_bytes(long long nseries, long long total, long long num_labels) {
+  return ragged_group_bytes(nseries < 0 ? 0 : nseries, total < 0 ? 0 : total, num_labels < 0 ? 0 : num_labels);
+}
+#define NBG_GRAGGED(NAME, FC, L, LS)                                                                 \
+  int nbg_group_##NAME##_ragged_f64_##LS(const double* values, const L* labels, const long long* offsets, \
+                                         long long nseries, long long total, long long num_labels,       \
+                                         double* out, void* ws, size_t ws_bytes, void* stream) {         \
+    return launch_ragged_group<FC, L>(values, labels, offsets, nseries, total, num_labels, out, ws,      \
+                                      ws_bytes, static_cast<cudaStream_t>(stream));                      \
+  }
+NBG_GRAGGED(nansum, kSum, int, i32)
+NBG_GRAGGED(nansum, kSum, long long, i64)
+NBG_GRAGGED(nanmean, kMean, int, i32)
+NBG_GRAGGED(nanmean, kMean, long long, i64)
+NBG_GRAGGED(nancount, kCount, int, i32)
+NBG_GRAGGED(nancount, kCount, long long, i64)
 }  // extern "C"

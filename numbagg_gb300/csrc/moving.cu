@@ -407,10 +407,10 @@ NBG_DEVICE int block_max(int v, int* buf) {  // result valid in every thread; bu
 
 template <int OP, typename T, bool C>
 __global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
-                                                     T* __restrict__ out, long long rows, long long n,
-                                                     long long window, long long min_count, long long chunk_len,
-                                                     long long chunks, const double* __restrict__ rcp,
-                                                     long long rcp_n, long long* __restrict__ first_bad) {
+                                                     T* __restrict__ out, Layout lay, long long window,
+                                                     long long min_count, long long chunk_len,
+                                                     const double* __restrict__ rcp, long long rcp_n,
+                                                     long long* __restrict__ first_bad) {
   constexpr int NS = Traits<OP>::NS;
   constexpr bool TWO = Traits<OP>::TWO;
   typedef typename BitsOf<T>::type B;
@@ -423,12 +423,16 @@ __global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, co
   __shared__ int red[2][NT / 32];
   const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long row = blockIdx.x / chunks, chunk = blockIdx.x - row * chunks;
-  const long long c0 = chunk * chunk_len, c1 = min(n, c0 + chunk_len);
-  const B* ar = as_bits(a) + row * n;
-  const B* br = TWO ? as_bits(b) + row * n : ar;
-  T* orow = out + row * n;
   const unsigned long long last_use = l2_evict_first();
+  const long long items = layout_items(lay);
+  // a persistent grid walks the chunks (of rows, or of ragged series)
+  for (long long id = blockIdx.x; id < items; id += gridDim.x) {
+  const Item it = layout_item(lay, id);
+  const long long row = it.row, n = it.len;
+  const long long c0 = it.index * chunk_len, c1 = min(n, c0 + chunk_len);
+  const B* ar = as_bits(a) + it.base;
+  const B* br = TWO ? as_bits(b) + it.base : ar;
+  T* orow = out + it.base;
 
   // ---- the state entering the chunk: the window [c0 - w, c0) ----
   const long long h0 = c0 > window ? c0 - window : 0;
@@ -532,6 +536,8 @@ __global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, co
   for (int o = 16; o > 0; o >>= 1) bad_pos = min(bad_pos, __shfl_xor_sync(0xffffffffu, bad_pos, o));
   if (lane == 0 && bad_pos != LLONG_MAX) atomicMin(reinterpret_cast<unsigned long long*>(first_bad + row),
                                                    static_cast<unsigned long long>(bad_pos));
+  __syncthreads();  // the shared state is reused by the next chunk
+  }
 }
 
 // reciprocal table and per-row first infinity, once per call
@@ -546,14 +552,15 @@ __global__ void move_setup_kernel(double* __restrict__ rcp, long long rcp_n, lon
 // The reference never recovers from an infinity (inf - inf = NaN in its running sums):
 // NaN from the first position where one has left the window (sum, mean) or entered it.
 template <typename T, bool VARLIKE>
-__global__ void move_poison_kernel(T* __restrict__ out, long long rows, long long n, long long window,
+__global__ void move_poison_kernel(T* __restrict__ out, Layout lay, long long window,
                                    const long long* __restrict__ first_bad) {
-  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+  for (long long r = blockIdx.x; r < lay.rows; r += gridDim.x) {
     const long long f = first_bad[r];
     if (f == LLONG_MAX) continue;
+    const long long n = layout_row_len(lay, r), base = layout_row_base(lay, r);
     const long long from = VARLIKE ? f : (f > LLONG_MAX - window ? LLONG_MAX : f + window);
     const T nan = quiet_nan(T(0));
-    for (long long i = (from < n ? from : n) + threadIdx.x; i < n; i += blockDim.x) out[r * n + i] = nan;
+    for (long long i = (from < n ? from : n) + threadIdx.x; i < n; i += blockDim.x) out[base + i] = nan;
   }
 }
 
@@ -568,53 +575,81 @@ using namespace nbg::moving;
 
 namespace {
 
-long long rcp_entries(long long n) { return n < kRcpEntries ? n : kRcpEntries; }
+size_t move_scratch_bytes(long long rows, long long) {
+  return 256 + static_cast<size_t>(kRcpEntries + 1) * 8 + 256 + static_cast<size_t>(rows) * 8 + 256 +
+         static_cast<size_t>(rows + 1) * 8;
+}
 
-size_t move_scratch_bytes(long long rows, long long n) {
-  return 256 + static_cast<size_t>(rcp_entries(n) + 1) * 8 + 256 + static_cast<size_t>(rows) * 8;
+struct MoveScratch {
+  double* rcp;
+  long long* first_bad;
+  long long* item_start;
+};
+MoveScratch carve_move(void* ws, long long rows) {
+  auto up = [](size_t p) { return (p + 255) & ~static_cast<size_t>(255); };
+  MoveScratch m;
+  size_t p = up(reinterpret_cast<size_t>(ws));
+  m.rcp = reinterpret_cast<double*>(p);
+  p = up(p + static_cast<size_t>(kRcpEntries + 1) * 8);
+  m.first_bad = reinterpret_cast<long long*>(p);
+  p = up(p + static_cast<size_t>(rows) * 8);
+  m.item_start = reinterpret_cast<long long*>(p);
+  return m;
 }
 
 // Chunks of at least 8 windows (the seed re-reads one window per chunk), 16 sub-tiles
-// at least; smaller when the grid would not fill the GPU.
-long long chunk_len_for(long long rows, long long n, long long window) {
+// at least; smaller when the rows would not give four waves of two CTAs per SM.
+long long default_chunk_len(long long window) {
   const long long w8 = (window > (LLONG_MAX / 16) ? LLONG_MAX / 16 : window) * 8;
-  long long len = std::max<long long>(16LL * SUB, ((w8 + SUB - 1) / SUB) * SUB);
+  return std::max<long long>(16LL * SUB, ((w8 + SUB - 1) / SUB) * SUB);
+}
+long long chunk_len_for(long long rows, long long n, long long window) {
+  long long len = default_chunk_len(window);
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long want = 4LL * 2 * sms;  // CTAs: four waves of two per SM
+  const long long want = 4LL * 2 * sms;
   while (len > SUB && rows * ((n + len - 1) / len) < want)
     len = std::max<long long>(SUB, ((len / 2 + SUB - 1) / SUB) * SUB);
   return len;
 }
 
+// offsets == nullptr: rows x n; else ragged series (n unused), chunk_len 0 = default
 template <int OP, typename T, bool C>
-int launch_move(const T* a, const T* b, T* out, long long rows, long long n, long long window,
-                long long min_count, void* ws, size_t ws_bytes, cudaStream_t stream) {
-  if (rows < 0 || n < 0 || window <= 0 || min_count < 0) return kInvalidArgument;
-  if (rows == 0 || n == 0) return kOk;
+int launch_move(const T* a, const T* b, T* out, const long long* offsets, long long rows, long long n,
+                long long window, long long min_count, long long chunk_len, void* ws, size_t ws_bytes,
+                cudaStream_t stream) {
+  if (rows < 0 || n < 0 || window <= 0 || min_count < 0 || chunk_len < 0) return kInvalidArgument;
+  if (rows == 0 || (!offsets && n == 0)) return kOk;
   if (!a || !out || (Traits<OP>::TWO && !b)) return kInvalidArgument;
   if (!ws || ws_bytes < move_scratch_bytes(rows, n)) return kWorkspaceTooSmall;
-  unsigned char* base = static_cast<unsigned char*>(ws);
-  base = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(base) + 255) & ~static_cast<size_t>(255));
-  const long long rcp_n = rcp_entries(n);
-  double* rcp = reinterpret_cast<double*>(base);
-  long long* first_bad = reinterpret_cast<long long*>(
-      (reinterpret_cast<size_t>(base + (rcp_n + 1) * 8) + 255) & ~static_cast<size_t>(255));
-  const long long len = chunk_len_for(rows, n, window);
-  const long long chunks = (n + len - 1) / len;
-  if (rows * chunks > 0x7fffffffLL) return kUnsupported;
+  const MoveScratch sc = carve_move(ws, rows);
+  const long long rcp_n = std::min<long long>(window, kRcpEntries);
+  Layout lay{offsets, sc.item_start, rows, n, 0};
+  long long len;
+  int launches = 3;
+  long long grid_items;
+  if (!offsets) {
+    len = chunk_len ? ((chunk_len + SUB - 1) / SUB) * SUB : chunk_len_for(rows, n, window);
+    lay.items_per_row = (n + len - 1) / len;
+    grid_items = rows * lay.items_per_row;
+  } else {
+    len = chunk_len ? ((chunk_len + SUB - 1) / SUB) * SUB : default_chunk_len(window);
+    ragged_plan_kernel<<<1, 1024, 0, stream>>>(offsets, rows, len, sc.item_start);
+    ++launches;
+    grid_items = LLONG_MAX;
+  }
   const long long setup_items = std::max(rcp_n + 1, rows);
   move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
-      rcp, rcp_n, first_bad, rows);
+      sc.rcp, rcp_n, sc.first_bad, rows);
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
   auto kern = move_kernel<OP, T, C>;
   if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  kern<<<static_cast<int>(rows * chunks), NT, smem, stream>>>(a, b, out, rows, n, window, min_count, len, chunks, rcp,
-                                                              rcp_n, first_bad);
+  kern<<<layout_grid(grid_items, 4), NT, smem, stream>>>(a, b, out, lay, window, min_count, len, sc.rcp, rcp_n,
+                                                         sc.first_bad);
   move_poison_kernel<T, Traits<OP>::VARLIKE><<<static_cast<int>(std::min<long long>(rows, 4096)), 256, 0, stream>>>(
-      out, rows, n, window, first_bad);
-  note_launches(3);
+      out, lay, window, sc.first_bad);
+  note_launches(launches);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 }  // namespace
@@ -626,14 +661,14 @@ size_t nbg_move_workspace_bytes(long long rows, long long n) { return move_scrat
 #define NBG_MOVE1(NAME, OPC, T, SFX, C)                                                        \
   int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window,  \
                          long long min_count, void* ws, size_t ws_bytes, void* stream) {     \
-    return launch_move<OPC, T, C>(a, nullptr, out, rows, n, window, min_count, ws, ws_bytes, \
+    return launch_move<OPC, T, C>(a, nullptr, out, nullptr, rows, n, window, min_count, 0, ws, ws_bytes, \
                                static_cast<cudaStream_t>(stream));                          \
   }
 #define NBG_MOVE2(NAME, OPC, T, SFX, C)                                                        \
   int nbg_##NAME##_##SFX(const T* a, const T* b, T* out, long long rows, long long n,        \
                          long long window, long long min_count, void* ws, size_t ws_bytes,   \
                          void* stream) {                                                    \
-    return launch_move<OPC, T, C>(a, b, out, rows, n, window, min_count, ws, ws_bytes,       \
+    return launch_move<OPC, T, C>(a, b, out, nullptr, rows, n, window, min_count, 0, ws, ws_bytes, \
                                static_cast<cudaStream_t>(stream));                          \
   }
 
@@ -657,5 +692,23 @@ NBG_MOVE1(move_var, kVar, double, f64_fp32c, true)
 NBG_MOVE1(move_std, kStd, double, f64_fp32c, true)
 NBG_MOVE2(move_cov, kCov, double, f64_fp32c, true)
 NBG_MOVE2(move_corr, kCorr, double, f64_fp32c, true)
+
+// Ragged series: series s is values[offsets[s] : offsets[s + 1]] (nseries + 1 offsets,
+// on the device), out has the same layout; chunk_len 0 picks the default.
+#define NBG_MOVE_RAGGED(NAME, OPC, SFX, C)                                                      \
+  int nbg_##NAME##_ragged_##SFX(const double* values, const long long* offsets, long long nseries, \
+                                double* out, long long window, long long min_count,             \
+                                long long chunk_len, void* ws, size_t ws_bytes, void* stream) {  \
+    return launch_move<OPC, double, C>(values, nullptr, out, offsets, nseries, 0, window, min_count, \
+                                       chunk_len, ws, ws_bytes, static_cast<cudaStream_t>(stream)); \
+  }
+NBG_MOVE_RAGGED(move_sum, kSum, f64, false)
+NBG_MOVE_RAGGED(move_mean, kMean, f64, false)
+NBG_MOVE_RAGGED(move_var, kVar, f64, false)
+NBG_MOVE_RAGGED(move_std, kStd, f64, false)
+NBG_MOVE_RAGGED(move_sum, kSum, f64_fp32c, true)
+NBG_MOVE_RAGGED(move_mean, kMean, f64_fp32c, true)
+NBG_MOVE_RAGGED(move_var, kVar, f64_fp32c, true)
+NBG_MOVE_RAGGED(move_std, kStd, f64_fp32c, true)
 
 }  // extern "C"

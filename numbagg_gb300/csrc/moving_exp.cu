@@ -28,6 +28,9 @@
 // value per element (numbagg/decorators.py:398-409).
 #include "dfloat.cuh"
 
+#include <algorithm>
+#include <climits>
+
 namespace nbg {
 namespace mexp {
 
@@ -293,8 +296,8 @@ template <int OP, typename T, typename N, int PHASE>
 __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, const T* __restrict__ b,
                                                       const T* __restrict__ alpha_arr, double alpha_scalar,
                                                       int alpha_mode, double min_weight,
-                                                      T* __restrict__ out, long long rows, long long n,
-                                                      long long tiles_per_row, Map<Traits<OP>::NS, N>* maps,
+                                                      T* __restrict__ out, Layout lay,
+                                                      Map<Traits<OP>::NS, N>* maps,
                                                       const Map<Traits<OP>::NS, N>* carries,
                                                       const double* __restrict__ pivots) {
   constexpr int NS = Traits<OP>::NS;
@@ -308,14 +311,16 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
   __shared__ B sy[TWO ? SPAD : 1];
   __shared__ B sa[SPAD];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long tile = blockIdx.x;
-  const long long row = tile / tiles_per_row;
-  const long long chunk = tile - row * tiles_per_row;
-  const long long t0 = chunk * TILE;
-  const B* ar = as_bits(a) + row * n;
-  const B* br = TWO ? as_bits(b) + row * n : nullptr;
-  const B* alr = alpha_mode == 2 ? as_bits(alpha_arr) + row * n : as_bits(alpha_arr);
   const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  const long long items = layout_items(lay);
+  // a persistent grid walks the tiles (of rows, or of ragged series)
+  for (long long tile = blockIdx.x; tile < items; tile += gridDim.x) {
+  const Item it = layout_item(lay, tile);
+  const long long row = it.row, n = it.len;
+  const long long t0 = it.index * TILE;
+  const B* ar = as_bits(a) + it.base;
+  const B* br = TWO ? as_bits(b) + it.base : nullptr;
+  const B* alr = alpha_mode == 2 ? as_bits(alpha_arr) + it.base : as_bits(alpha_arr);
 
   // ---- stage the tile (coalesced), then each thread takes 8 consecutive positions ----
 #pragma unroll
@@ -401,7 +406,8 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
   __syncthreads();
   if (PHASE == 0) {
     if (tid == 0) maps[tile] = warp_tot[NT / 32 - 1];
-    return;
+    __syncthreads();  // the stage and warp_tot are reused by the next tile
+    continue;
   }
   if (warp > 0) excl = compose<OP, N>(warp_tot[warp - 1], excl);
   // state entering this thread = (excl o carry) applied to the zero state
@@ -432,11 +438,14 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
                                       : static_cast<B>(__float_as_uint(static_cast<float>(rt)));
   }
   __syncthreads();
-  B* ob = as_bits(out) + row * n;
+  B* ob = as_bits(out) + it.base;
 #pragma unroll
   for (int j = 0; j < KT; ++j) {
     const int p = j * NT + tid;
     if (t0 + p < n) ob[t0 + p] = sx[spad(p)];
+  }
+  __syncthreads();  // the stage and warp_tot are reused by the next tile
+  (void)row;
   }
 }
 
@@ -444,15 +453,17 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
 // order (a block-wide scan over chunks of NT tiles), so the carries are reproducible.
 template <int OP, typename N>
 __global__ void __launch_bounds__(NT) exp_carry_kernel(const Map<Traits<OP>::NS, N>* __restrict__ maps,
-                                                       Map<Traits<OP>::NS, N>* __restrict__ carries,
-                                                       long long tiles_per_row) {
+                                                       Map<Traits<OP>::NS, N>* __restrict__ carries, Layout lay) {
   using M = Map<Traits<OP>::NS, N>;
   __shared__ M warp_tot[NT / 32];
   __shared__ M running_smem;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long row = blockIdx.x;
-  const M* mr = maps + row * tiles_per_row;
-  M* cr = carries + row * tiles_per_row;
+  for (long long row = blockIdx.x; row < lay.rows; row += gridDim.x) {
+  const long long first = lay.offsets ? lay.item_start[row] : row * lay.items_per_row;
+  const long long tiles_per_row = lay.offsets ? lay.item_start[row + 1] - first : lay.items_per_row;
+  const M* mr = maps + first;
+  M* cr = carries + first;
+  __syncthreads();
   if (threadIdx.x == 0) running_smem = identity_map<OP, N>();
   __syncthreads();
   for (long long base = 0; base < tiles_per_row; base += NT) {
@@ -488,18 +499,20 @@ __global__ void __launch_bounds__(NT) exp_carry_kernel(const Map<Traits<OP>::NS,
     if (threadIdx.x == 0) running_smem = compose<OP, N>(running, warp_tot[NT / 32 - 1]);
     __syncthreads();
   }
+  }
 }
 
 // The pivot of each row (and of b): its first finite value, 0 if none.  One warp per row.
 template <typename T>
-__global__ void exp_pivot_kernel(const T* __restrict__ a, const T* __restrict__ b, long long rows, long long n,
+__global__ void exp_pivot_kernel(const T* __restrict__ a, const T* __restrict__ b, Layout lay,
                                  double* __restrict__ pivots) {
   typedef typename BitsOf<T>::type B;
   const int lane = threadIdx.x & 31;
   const long long row = static_cast<long long>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (row >= rows) return;
+  if (row >= lay.rows) return;
+  const long long n = layout_row_len(lay, row);
   for (int which = 0; which < (b ? 2 : 1); ++which) {
-    const B* r = as_bits(which ? b : a) + row * n;
+    const B* r = as_bits(which ? b : a) + layout_row_base(lay, row);
     double p = 0.0;
     for (long long base = 0; base < n; base += 32) {
       const long long i = base + lane;
@@ -527,41 +540,49 @@ namespace {
 
 long long exp_tiles_per_row(long long n) { return n <= 0 ? 0 : (n + TILE - 1) / TILE; }
 
-template <int OP>
-size_t exp_scratch_bytes(long long rows, long long n) {
-  return 2 * static_cast<size_t>(rows * exp_tiles_per_row(n)) * sizeof(Map<Traits<OP>::NS, F64>) + 512 +
-         static_cast<size_t>(rows) * 16;
+// maps and carries for `tiles` tiles, pivots and the ragged plan for `rows` series
+size_t exp_scratch_for(long long rows, long long tiles) {
+  return 2 * static_cast<size_t>(tiles) * sizeof(Map<Traits<kCorr>::NS, F64>) + 1024 +
+         static_cast<size_t>(rows) * 16 + static_cast<size_t>(rows + 1) * 8;
 }
 
+// offsets == nullptr: rows x n; else ragged series with `total` values in all
 template <int OP, typename T, typename N>
 int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int alpha_mode,
-               double min_weight, T* out, long long rows, long long n, void* ws, size_t ws_bytes,
-               cudaStream_t s) {
-  if (rows < 0 || n < 0 || alpha_mode < 0 || alpha_mode > 2) return kInvalidArgument;
-  if (rows == 0 || n == 0) return kOk;
+               double min_weight, T* out, const long long* offsets, long long rows, long long n, long long total,
+               void* ws, size_t ws_bytes, cudaStream_t s) {
+  if (rows < 0 || n < 0 || total < 0 || alpha_mode < 0 || alpha_mode > 2) return kInvalidArgument;
+  if (offsets && alpha_mode == 1) return kInvalidArgument;  // one alpha per position needs equal lengths
+  if (rows == 0 || (!offsets && n == 0)) return kOk;
   if (!a || !out || (Traits<OP>::TWO && !b) || (alpha_mode > 0 && !alpha)) return kInvalidArgument;
-  const long long tpr = exp_tiles_per_row(n);
-  const long long total = rows * tpr;
-  if (total > 0x7fffffffll) return kUnsupported;
-  if (!ws || ws_bytes < exp_scratch_bytes<OP>(rows, n)) return kWorkspaceTooSmall;
+  // an upper bound on the tiles: each series adds at most one partial tile
+  const long long tiles = offsets ? total / TILE + rows : rows * exp_tiles_per_row(n);
+  if (!ws || ws_bytes < exp_scratch_for(rows, tiles)) return kWorkspaceTooSmall;
   using M = Map<Traits<OP>::NS, N>;
-  static_assert(sizeof(M) == sizeof(Map<Traits<OP>::NS, F64>), "both policies use 8-byte numbers");
-  M* maps = reinterpret_cast<M*>((reinterpret_cast<size_t>(ws) + 127) & ~static_cast<size_t>(127));
-  M* carries = maps + total;
-  double* pivots = reinterpret_cast<double*>((reinterpret_cast<size_t>(carries + total) + 127) & ~static_cast<size_t>(127));
+  static_assert(sizeof(M) <= sizeof(Map<Traits<kCorr>::NS, F64>), "8-byte numbers");
+  auto up = [](size_t p) { return (p + 255) & ~static_cast<size_t>(255); };
+  M* maps = reinterpret_cast<M*>(up(reinterpret_cast<size_t>(ws)));
+  M* carries = maps + tiles;
+  double* pivots = reinterpret_cast<double*>(up(reinterpret_cast<size_t>(carries + tiles)));
+  long long* item_start = reinterpret_cast<long long*>(up(reinterpret_cast<size_t>(pivots + 2 * rows)));
+  Layout lay{offsets, item_start, rows, n, offsets ? 0 : exp_tiles_per_row(n)};
   int launches = 3;
-  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
-  if (SHIFT) {
-    exp_pivot_kernel<T><<<static_cast<int>((rows + 7) / 8), 256, 0, s>>>(a, Traits<OP>::TWO ? b : nullptr, rows, n,
-                                                                        pivots);
+  if (offsets) {
+    ragged_plan_kernel<<<1, 1024, 0, s>>>(offsets, rows, TILE, item_start);
     ++launches;
   }
-  const int grid = static_cast<int>(total);
-  exp_tile_kernel<OP, T, N, 0><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n,
-                                                   tpr, maps, carries, pivots);
-  exp_carry_kernel<OP, N><<<static_cast<int>(rows), NT, 0, s>>>(maps, carries, tpr);
-  exp_tile_kernel<OP, T, N, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n,
-                                                   tpr, maps, carries, pivots);
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  if (SHIFT) {
+    exp_pivot_kernel<T><<<static_cast<int>((rows + 7) / 8), 256, 0, s>>>(a, Traits<OP>::TWO ? b : nullptr, lay, pivots);
+    ++launches;
+  }
+  // rows: one CTA per tile; ragged series: a persistent grid over the planned tiles
+  const int grid = offsets ? layout_grid(LLONG_MAX, 16) : static_cast<int>(std::min<long long>(tiles, 0x7fffffffLL));
+  exp_tile_kernel<OP, T, N, 0><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, lay, maps,
+                                                   carries, pivots);
+  exp_carry_kernel<OP, N><<<static_cast<int>(std::min<long long>(rows, 65535)), NT, 0, s>>>(maps, carries, lay);
+  exp_tile_kernel<OP, T, N, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, lay, maps,
+                                                   carries, pivots);
   note_launches(launches);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
@@ -571,7 +592,11 @@ extern "C" {
 
 // the largest state (move_exp_nancorr) bounds every function's scratch
 size_t nbg_move_exp_workspace_bytes(long long rows, long long n) {
-  return exp_scratch_bytes<kCorr>(rows, n);
+  return exp_scratch_for(rows, rows * exp_tiles_per_row(n));
+}
+// ragged series holding `total` values in all
+size_t nbg_move_exp_ragged_workspace_bytes(long long nseries, long long total) {
+  return exp_scratch_for(nseries, total / TILE + nseries);
 }
 
 // alpha_mode: 0 = scalar `alpha_scalar`, 1 = `alpha` has n values shared by all rows,
@@ -581,14 +606,14 @@ size_t nbg_move_exp_workspace_bytes(long long rows, long long n) {
                          double min_weight, T* out, long long rows, long long n, void* ws,        \
                          size_t ws_bytes, void* stream) {                                         \
     return launch_exp<OPC, T, N>(a, nullptr, alpha, alpha_scalar, alpha_mode, min_weight, out,   \
-                                 rows, n, ws, ws_bytes, static_cast<cudaStream_t>(stream));      \
+                                 nullptr, rows, n, 0, ws, ws_bytes, static_cast<cudaStream_t>(stream)); \
   }
 #define NBG_EXP2(NAME, OPC, T, SFX, N)                                                           \
   int nbg_##NAME##_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,             \
                          int alpha_mode, double min_weight, T* out, long long rows, long long n,   \
                          void* ws, size_t ws_bytes, void* stream) {                               \
-    return launch_exp<OPC, T, N>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, rows, n, \
-                                 ws, ws_bytes, static_cast<cudaStream_t>(stream));               \
+    return launch_exp<OPC, T, N>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, nullptr, rows, \
+                                 n, 0, ws, ws_bytes, static_cast<cudaStream_t>(stream));          \
   }
 
 NBG_EXP1(move_exp_nancount, kCount, double, f64, F64)
@@ -613,5 +638,24 @@ NBG_EXP1(move_exp_nanvar, kVar, double, f64_fp32c, DF)
 NBG_EXP1(move_exp_nanstd, kStd, double, f64_fp32c, DF)
 NBG_EXP2(move_exp_nancov, kCov, double, f64_fp32c, DF)
 NBG_EXP2(move_exp_nancorr, kCorr, double, f64_fp32c, DF)
+
+// Ragged series: series s is values[offsets[s] : offsets[s + 1]] (nseries + 1 offsets on
+// the device, `total` = offsets[nseries]); a scalar alpha (alpha_mode 0) or one per
+// value (alpha_mode 2).
+#define NBG_EXP_RAGGED(NAME, OPC, SFX, N)                                                          \
+  int nbg_##NAME##_ragged_##SFX(const double* values, const long long* offsets, long long nseries,   \
+                                long long total, const double* alpha, double alpha_scalar,          \
+                                int alpha_mode, double min_weight, double* out, void* ws,           \
+                                size_t ws_bytes, void* stream) {                                    \
+    return launch_exp<OPC, double, N>(values, nullptr, alpha, alpha_scalar, alpha_mode, min_weight, \
+                                      out, offsets, nseries, 0, total, ws, ws_bytes,                \
+                                      static_cast<cudaStream_t>(stream));                           \
+  }
+NBG_EXP_RAGGED(move_exp_nanmean, kMean, f64, F64)
+NBG_EXP_RAGGED(move_exp_nanvar, kVar, f64, F64)
+NBG_EXP_RAGGED(move_exp_nanstd, kStd, f64, F64)
+NBG_EXP_RAGGED(move_exp_nanmean, kMean, f64_fp32c, DF)
+NBG_EXP_RAGGED(move_exp_nanvar, kVar, f64_fp32c, DF)
+NBG_EXP_RAGGED(move_exp_nanstd, kStd, f64_fp32c, DF)
 
 }  // extern "C"

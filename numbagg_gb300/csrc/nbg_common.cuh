@@ -386,3 +386,58 @@ NBG_DEVICE T block_broadcast(T v, T* smem_slot) {
 }
 
 }  // namespace nbg
+
+namespace nbg {
+
+// ---------------------------------------------------------------------------------
+// rectangular rows or ragged series
+// ---------------------------------------------------------------------------------
+// A batch is either `rows` rows of `n` values (offsets == nullptr) or `rows` series of
+// uneven length in one flat buffer, series s covering [offsets[s], offsets[s + 1]).
+// Kernels walk work items (chunks or tiles of a series); for ragged batches
+// `item_start[s]` is the first item of series s and item_start[rows] the total, as
+// computed on the device by ragged_plan_kernel, so launches need no host round trip.
+struct Layout {
+  const long long* offsets;
+  const long long* item_start;
+  long long rows, n, items_per_row;
+};
+struct Item {
+  long long row, index, base, len;  // series, item within it, first element, series length
+};
+NBG_DEVICE long long layout_items(const Layout& L) {
+  return L.offsets ? L.item_start[L.rows] : L.rows * L.items_per_row;
+}
+NBG_DEVICE Item layout_item(const Layout& L, long long id) {
+  Item it;
+  if (!L.offsets) {
+    it.row = id / L.items_per_row;
+    it.index = id - it.row * L.items_per_row;
+    it.base = it.row * L.n;
+    it.len = L.n;
+    return it;
+  }
+  long long lo = 0, hi = L.rows - 1;  // last series whose first item is <= id
+  while (lo < hi) {
+    const long long mid = (lo + hi + 1) >> 1;
+    if (L.item_start[mid] <= id) lo = mid;
+    else hi = mid - 1;
+  }
+  it.row = lo;
+  it.index = id - L.item_start[lo];
+  it.base = L.offsets[lo];
+  it.len = L.offsets[lo + 1] - it.base;
+  return it;
+}
+NBG_DEVICE long long layout_row_len(const Layout& L, long long r) {
+  return L.offsets ? L.offsets[r + 1] - L.offsets[r] : L.n;
+}
+NBG_DEVICE long long layout_row_base(const Layout& L, long long r) { return L.offsets ? L.offsets[r] : r * L.n; }
+
+// item_start[s] = sum over earlier series of ceil(len / item_len); one CTA of 1024 threads
+__global__ void ragged_plan_kernel(const long long* __restrict__ offsets, long long rows, long long item_len,
+                                   long long* __restrict__ item_start);
+// persistent grid for a layout: `per_sm` CTAs per SM, fewer when the items are fewer
+int layout_grid(long long max_items, int per_sm);
+
+}  // namespace nbg
