@@ -54,7 +54,7 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cols", type=int, default=COLS, help="columns (smaller for quick runs)")
@@ -470,7 +470,11 @@ def run_ours(args):
 
 def run_e2e(args, nb, values, labels, fill, calls, device, world):
     """The same step through the public API with host buffers: every step copies its
-    inputs from pinned host memory and reads every result back into pinned memory."""
+    inputs from pinned host memory and reads every result back into pinned memory.
+    Three streams overlap the work as a production pipeline would: host-to-device copies
+    (into double-buffered device inputs, so step k+1's inputs arrive while step k
+    computes), the calls, and device-to-host copies of each result as soon as its call
+    has finished."""
     import torch
 
     h_values = torch.empty(values.shape, dtype=values.dtype, pin_memory=True)
@@ -478,35 +482,66 @@ def run_e2e(args, nb, values, labels, fill, calls, device, world):
     h_values.copy_(values)
     h_fill.copy_(fill)
     h_labels = {K: torch.empty(labels[K].shape, dtype=labels[K].dtype, pin_memory=True).copy_(labels[K]) for K in KS}
-    out_bytes = {}
     h_out_fill = torch.empty(fill.shape, dtype=fill.dtype, pin_memory=True)
     h_out_group = {K: torch.empty((values.shape[0], K), dtype=torch.float64, pin_memory=True) for K in KS}
-    stream = torch.cuda.current_stream(device)
+    comp = torch.cuda.current_stream(device)
+    s_in = torch.cuda.Stream(device)
+    s_out = torch.cuda.Stream(device)
+    # the fill calls first: their outputs are most of the bytes read back, so the
+    # device-to-host stream starts as early as possible in each step
+    calls = [c for c in calls if c[1][0] == "fill"] + [c for c in calls if c[1][0] != "fill"]
     h2d = values.numel() * 8 + fill.numel() * 8 + sum(labels[K].numel() * 4 for K in KS)
     d2h = 0
     for _, (kind, f, arg), _ in calls:
         d2h += fill.numel() * 8 if kind == "fill" else values.shape[0] * arg * 8
-    del out_bytes
+    # two sets of device inputs (the timed values/fill tensors are reused as one of them)
+    sets = [
+        (values, fill, dict(labels)),
+        (torch.empty_like(values), torch.empty_like(fill), {K: torch.empty_like(labels[K]) for K in KS}),
+    ]
+    released = [None, None]  # compute-stream event after the last use of each set
+    drained = {}  # device-to-host event after each step's last read-back
 
-    def step():
-        d_values = h_values.to(device, non_blocking=True)
-        d_fill = h_fill.to(device, non_blocking=True)
-        d_labels = {K: h_labels[K].to(device, non_blocking=True) for K in KS}
+    def step(k):
+        d_values, d_fill, d_labels = sets[k % 2]
+        # at most two steps of results waiting for the read-back (bounds device memory)
+        if k - 2 in drained:
+            comp.wait_event(drained.pop(k - 2))
+        with torch.cuda.stream(s_in):
+            if released[k % 2] is not None:
+                s_in.wait_event(released[k % 2])
+            d_fill.copy_(h_fill, non_blocking=True)
+            ev_fill = s_in.record_event()
+            d_values.copy_(h_values, non_blocking=True)
+            for K in KS:
+                d_labels[K].copy_(h_labels[K], non_blocking=True)
+            ev_group = s_in.record_event()
+        comp.wait_event(ev_fill)
         for _, spec, _ in calls:
-            r = run_call(nb, spec, d_values, d_labels, d_fill)
             kind, f, arg = spec
-            (h_out_fill if kind == "fill" else h_out_group[arg]).copy_(r, non_blocking=True)
-        return d_values, d_fill
+            if kind == "group":
+                comp.wait_event(ev_group)
+            r = run_call(nb, spec, d_values, d_labels, d_fill)
+            done = comp.record_event()
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(done)
+                (h_out_fill if kind == "fill" else h_out_group[arg]).copy_(r, non_blocking=True)
+                r.record_stream(s_out)
+        released[k % 2] = comp.record_event()
+        drained[k] = s_out.record_event()
 
-    step()
+    step(0)
     torch.cuda.synchronize(device)
     barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(args.e2e_steps):
-        step()
-    t1.record(stream)
+    t0.record(comp)
+    s_in.wait_event(t0)
+    for k in range(args.e2e_steps):
+        step(k + 1)
+    comp.wait_stream(s_in)
+    comp.wait_stream(s_out)
+    t1.record(comp)
     torch.cuda.synchronize(device)
     barrier()
     ms = reduce_max(t0.elapsed_time(t1) / args.e2e_steps, device)
@@ -518,6 +553,7 @@ def run_e2e(args, nb, values, labels, fill, calls, device, world):
         "d2h_bytes_per_step": int(d2h),
         "ms_per_step": round(ms, 3),
         "steps": args.e2e_steps,
+        "streams": "host-to-device, compute, device-to-host (overlapped; inputs double-buffered)",
     }
 
 

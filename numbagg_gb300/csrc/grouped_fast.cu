@@ -459,15 +459,31 @@ __global__ void __launch_bounds__(FT) chunk_hist_kernel(const L* __restrict__ la
   __syncthreads();
   for (int k = threadIdx.x; k < K; k += FT) hist[chunk * K + k] = hsm[k];
 }
-// whole row (large path): hist[k]
+// whole row (large path): hist[k], and the table rcp[c] = RN(1 / c) for c <= kRcpN
+constexpr long long kRcpN = 1 << 16;
 template <typename L>
 __global__ void __launch_bounds__(FT) row_hist_kernel(const L* __restrict__ labels, long long m, long long K,
-                                                      unsigned* __restrict__ hist) {
+                                                      unsigned* __restrict__ hist, double* __restrict__ rcp) {
   const long long stride = static_cast<long long>(gridDim.x) * FT;
-  for (long long c = static_cast<long long>(blockIdx.x) * FT + threadIdx.x; c < m; c += stride) {
+  const long long t0 = static_cast<long long>(blockIdx.x) * FT + threadIdx.x;
+  for (long long c = t0; c <= kRcpN; c += stride) rcp[c] = c ? 1.0 / static_cast<double>(c) : 0.0;
+  for (long long c = t0; c < m; c += stride) {
     const long long l = static_cast<long long>(labels[c]);
     if (l >= 0 && l < K) atomicAdd(&hist[l], 1u);
   }
+}
+
+// s / c for a count c >= 1, correctly rounded: Markstein's FMA correction of s * RN(1/c)
+// with the reciprocal from the table (three FP64 operations instead of a division);
+// beyond the table, and for infinite or NaN s, a division
+NBG_DEVICE double div_by_count(double s, long long c, const double* __restrict__ rcp) {
+  const bool finite = (static_cast<unsigned long long>(__double_as_longlong(s)) & 0x7ff0000000000000ull) !=
+                      0x7ff0000000000000ull;
+  if (c > kRcpN || !finite) return s / static_cast<double>(c);
+  const double r = __ldg(rcp + c);
+  const double q0 = s * r;
+  const double e = fma(-q0, static_cast<double>(c), s);
+  return fma(e, r, q0);
 }
 
 // ---------------------------------------------------------------------------------
@@ -992,7 +1008,8 @@ __global__ void ragged_fold_kernel(const MomPart* __restrict__ parts, double* __
 template <int F, typename O, int RB>
 __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
                                       const unsigned* __restrict__ nanc, const unsigned* __restrict__ hist,
-                                      O* __restrict__ out, long long rows, long long K, long long ddof) {
+                                      const double* __restrict__ rcp, O* __restrict__ out, long long rows,
+                                      long long K, long long ddof) {
   const long long total = (rows + RB - 1) / RB * K * RB;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < total; t += stride) {
@@ -1008,10 +1025,10 @@ __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const dou
     if (F == kCount) res = static_cast<O>(cnt);
     else if (F == kSum) res = static_cast<O>(s1);
     else if (F == kSumSq) res = static_cast<O>(s2);
-    else if (F == kMean) res = static_cast<O>(cnt == 0 ? nan : s1 / static_cast<double>(cnt));
+    else if (F == kMean) res = static_cast<O>(cnt == 0 ? nan : div_by_count(s1, cnt, rcp));
     else {
       const long long denom = cnt - ddof;
-      double v = denom <= 0 ? nan : (s2 - (s1 * s1) / static_cast<double>(cnt)) / static_cast<double>(denom);
+      double v = denom <= 0 ? nan : div_by_count(s2 - div_by_count(s1 * s1, cnt, rcp), denom, rcp);
       if (F == kStd) v = sqrt(v);
       res = static_cast<O>(v);
     }
@@ -1146,7 +1163,7 @@ inline size_t fast_bytes(int f, long long rows, long long m, long long K) {
   const FastPlan p = fast_plan(f, rows, m, K);
   if (p.strategy == 2) {
     const size_t slots = static_cast<size_t>(p.blocks * p.rb * K);
-    if (is_moments(f)) return slots * (8 + 8 + 4) + static_cast<size_t>(K) * 4 + 1024;
+    if (is_moments(f)) return slots * (8 + 8 + 4) + static_cast<size_t>(K) * 4 + (kRcpN + 1) * 8 + 1280;
     return slots * 16 + 1024;
   }
   const size_t part = is_moments(f) ? sizeof(MomPart) : sizeof(SelPart);
@@ -1188,18 +1205,19 @@ int launch_big_mom(const V* values, const L* labels, O* out, long long rows, lon
   double* acc2 = carve<double>(cur, Need<F>::s2 ? slots : 1);
   unsigned* nanc = carve<unsigned>(cur, slots);
   unsigned* hist = carve<unsigned>(cur, K);
+  double* rcp = carve<double>(cur, kRcpN + 1);
   int launches = 0;
   if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * 8, s);
   if (Need<F>::s2) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
   if (Need<F>::cnt) {
     cudaMemsetAsync(nanc, 0, static_cast<size_t>(slots) * 4, s);
     cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
-    row_hist_kernel<L><<<fin_grid(m), FT, 0, s>>>(labels, m, K, hist);
+    row_hist_kernel<L><<<fin_grid(max(m, kRcpN + 1)), FT, 0, s>>>(labels, m, K, hist, rcp);
     ++launches;
   }
   big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
                                                                                    p.chunks, acc1, acc2, nanc);
-  big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, out, rows, K, ddof);
+  big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
   return launches + 2;
 }
 
