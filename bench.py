@@ -61,10 +61,11 @@ def parse_args(argv=None):
     p.add_argument("--only", default=None, help="regex: time only the calls whose key matches (profiling)")
     p.add_argument(
         "--suite",
-        choices=("group_fill", "scan", "ragged"),
+        choices=("group_fill", "scan", "ragged", "link"),
         default="group_fill",
         help="group_fill: the headline workload; scan: the moving-window, EWM and matrix shapes; "
-        "ragged: the batched mix of series of uneven length",
+        "ragged: the batched mix of series of uneven length; link: pinned host<->device copy "
+        "bandwidth (the bound of the end-to-end number)",
     )
     p.add_argument("--ragged-series", type=int, default=20_000, help="series in the ragged batch")
     return p.parse_args(argv)
@@ -790,6 +791,68 @@ def run_ragged_suite(args):
     return 0
 
 
+def run_link_suite(args):
+    """Pinned host <-> device copy bandwidth through the copy engines (4 GiB per copy):
+    each direction alone, and both at once on two streams.  The end-to-end step moves
+    its inputs in and its results out over this link."""
+    import torch
+
+    world, rank, local = dist_env()
+    device = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+    n = 4 << 30
+    h_a = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    h_b = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    h_a.fill_(1)
+    h_b.fill_(2)
+    d_a = torch.empty(n, dtype=torch.uint8, device=device)
+    d_b = torch.empty(n, dtype=torch.uint8, device=device)
+    d_a.fill_(3)
+    s1, s2 = torch.cuda.Stream(device), torch.cuda.Stream(device)
+
+    def timed(fn):
+        best = None
+        for _ in range(max(3, args.steps)):
+            torch.cuda.synchronize(device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s1)
+            s2.wait_event(e0)
+            fn()
+            s1.wait_stream(s2)
+            e1.record(s1)
+            torch.cuda.synchronize(device)
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    def d2h():
+        with torch.cuda.stream(s1):
+            h_a.copy_(d_a, non_blocking=True)
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            d_b.copy_(h_b, non_blocking=True)
+
+    def both():
+        with torch.cuda.stream(s1):
+            h_a.copy_(d_a, non_blocking=True)
+        with torch.cuda.stream(s2):
+            d_b.copy_(h_b, non_blocking=True)
+
+    r_d2h, r_h2d, r_both = timed(d2h), timed(h2d), timed(both)
+    line = {
+        "suite": "link",
+        "metric": "pinned host<->device copy GB/s (best of the repetitions)",
+        "bytes_per_copy": n,
+        "d2h_GB/s": round(n / (r_d2h / 1e3) / 1e9, 1),
+        "h2d_GB/s": round(n / (r_h2d / 1e3) / 1e9, 1),
+        "both_directions_total_GB/s": round(2 * n / (r_both / 1e3) / 1e9, 1),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -798,6 +861,8 @@ def main(argv=None):
         return run_scan_suite(args)
     if args.suite == "ragged":
         return run_ragged_suite(args)
+    if args.suite == "link":
+        return run_link_suite(args)
     return run_ours(args)
 
 

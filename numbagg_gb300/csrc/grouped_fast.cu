@@ -37,7 +37,7 @@ namespace grouped {
 
 constexpr int FT = 256;
 constexpr int kTinyK = 16;
-constexpr int kTileCols = 32 * 16;   // columns of one warp tile (tiny path)
+constexpr int kTileCols = 32 * 16;   // tiny path: chunks are multiples of FT / 32 x kTileCols columns
 constexpr int kCtaCols = FT * 8;     // columns of one CTA tile (medium / large paths)
 
 struct MomPart {  // one bin of one chunk: float64 sums, valid count, infinities seen
@@ -212,8 +212,15 @@ NBG_DEVICE unsigned long long sel_key_of(V v) {
 // truncated: at most 2^-(52 - d1) of the largest value the warp met, per term.
 // At the end of the chunk the lanes' bins are summed exactly (128-bit) per warp and
 // rounded once to float64.
+// CTAs per SM the tiny moment kernels are compiled for: sums and means are bound by
+// integer issue and gain from a third CTA; the others measured faster with two
+template <int F>
+struct TinyOcc {
+  static constexpr int value = (F == kSum || F == kMean) ? 3 : 2;
+};
+
 template <int F, typename V, typename L>
-__global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+__global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                          long long rows, long long m, int K, long long chunk_len,
                                                          long long chunks, int d1, int d2,
                                                          MomPart* __restrict__ parts) {
@@ -241,21 +248,30 @@ __global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ v
   __syncthreads();
   const B* vr = as_bits(values) + row * m;
   int E = 0;  // the warp's scale (uniform across the warp)
-  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
-       base += static_cast<long long>(FT / 32) * kTileCols) {
-    B v[16];
-    int lab[16];
+  // Warp tiles of 32 x J columns, the next tile's loads issued before the current tile
+  // is reduced, so each warp always has a tile in flight.
+  constexpr int J = 8;
+  constexpr long long TC = 32 * J, STEP = static_cast<long long>(FT / 32) * TC;
+  auto load = [&](long long base, B (&v)[J], int (&lab)[J]) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < J; ++j) {
       const long long col = base + j * 32 + lane;
       const bool in = col < c1;
       v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
       lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
     }
+  };
+  B v[J];
+  int lab[J];
+  load(c0 + warp * TC, v, lab);
+  for (long long base = c0 + warp * TC; base < c1; base += STEP) {
+    B vn[J];
+    int ln[J];
+    load(base + STEP, vn, ln);
     int emax = 0;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < J; ++j) {
       if (nan_bits(v[j])) lab[j] = -1;
       if (MOM) {
         const Dec d = decomp(v[j]);
@@ -277,7 +293,7 @@ __global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ v
       }
     }
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < J; ++j) {
       if (lab[j] < 0) continue;
       const int slot = lab[j] * FT + tid;
       if (CNT) bc[slot] += 1;
@@ -301,6 +317,11 @@ __global__ void __launch_bounds__(FT, 2) tiny_mom_kernel(const V* __restrict__ v
         }
         b2[slot] += q;
       }
+    }
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      v[j] = vn[j];
+      lab[j] = ln[j];
     }
   }
   // lanes' bins -> exact warp sums -> float64 at the warp's scale
@@ -375,22 +396,30 @@ __global__ void __launch_bounds__(FT, 2) tiny_sel_kernel(const V* __restrict__ v
     bi[k * FT + tid] = ~0ull;
   }
   const B* vr = as_bits(values) + row * m;
-  for (long long base = c0 + static_cast<long long>(warp) * kTileCols; base < c1;
-       base += static_cast<long long>(FT / 32) * kTileCols) {
-    B v[16];
-    int lab[16];
+  // warp tiles of 32 x J columns, the next tile's loads in flight while one is reduced
+  constexpr int J = 8;
+  constexpr long long TC = 32 * J, STEP = static_cast<long long>(FT / 32) * TC;
+  auto load = [&](long long base, B (&v)[J], int (&lab)[J]) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < J; ++j) {
       const long long col = base + j * 32 + lane;
       const bool in = col < c1;
       v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
-      lab[j] = (l >= 0 && l < K && !nan_bits(v[j])) ? static_cast<int>(l) : -1;
+      lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
     }
+  };
+  B v[J];
+  int lab[J];
+  load(c0 + warp * TC, v, lab);
+  for (long long base = c0 + warp * TC; base < c1; base += STEP) {
+    B vn[J];
+    int ln[J];
+    load(base + STEP, vn, ln);
     // a lane meets its columns in increasing order
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      if (lab[j] < 0) continue;
+    for (int j = 0; j < J; ++j) {
+      if (lab[j] < 0 || nan_bits(v[j])) continue;
       const int slot = lab[j] * FT + tid;
       const unsigned long long c = static_cast<unsigned long long>(base + j * 32 + lane);
       if (F == kFirst) {
@@ -404,6 +433,11 @@ __global__ void __launch_bounds__(FT, 2) tiny_sel_kernel(const V* __restrict__ v
           bi[slot] = c;
         }
       }
+    }
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      v[j] = vn[j];
+      lab[j] = ln[j];
     }
   }
   // reduce lanes, then warps (fixed order)
@@ -459,17 +493,30 @@ __global__ void __launch_bounds__(FT) chunk_hist_kernel(const L* __restrict__ la
   __syncthreads();
   for (int k = threadIdx.x; k < K; k += FT) hist[chunk * K + k] = hsm[k];
 }
-// whole row (large path): hist[k], and the table rcp[c] = RN(1 / c) for c <= kRcpN
+// whole row (large path): hist[k], and the table rcp[c] = RN(1 / c) for c <= kRcpN.
+// Up to kHistSmem labels each CTA counts its share in shared memory first (many
+// columns per label: global atomics on few addresses would serialise).
 constexpr long long kRcpN = 1 << 16;
-template <typename L>
+constexpr int kHistSmem = 16384;
+template <typename L, bool SMEM>
 __global__ void __launch_bounds__(FT) row_hist_kernel(const L* __restrict__ labels, long long m, long long K,
                                                       unsigned* __restrict__ hist, double* __restrict__ rcp) {
+  extern __shared__ unsigned hsm[];
   const long long stride = static_cast<long long>(gridDim.x) * FT;
   const long long t0 = static_cast<long long>(blockIdx.x) * FT + threadIdx.x;
   for (long long c = t0; c <= kRcpN; c += stride) rcp[c] = c ? 1.0 / static_cast<double>(c) : 0.0;
+  if (SMEM) {
+    for (int k = threadIdx.x; k < K; k += FT) hsm[k] = 0;
+    __syncthreads();
+  }
   for (long long c = t0; c < m; c += stride) {
     const long long l = static_cast<long long>(labels[c]);
-    if (l >= 0 && l < K) atomicAdd(&hist[l], 1u);
+    if (l >= 0 && l < K) atomicAdd(SMEM ? &hsm[l] : &hist[l], 1u);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += FT)
+      if (hsm[k]) atomicAdd(&hist[k], hsm[k]);
   }
 }
 
@@ -779,11 +826,16 @@ NBG_DEVICE long long big_col(long long cbase, int e) {
 template <int F, typename V, typename L, int RB>
 __global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                      long long rows, long long m, long long K, long long chunk_len,
-                                                     long long chunks, double* __restrict__ acc1,
-                                                     double* __restrict__ acc2, unsigned* __restrict__ nanc) {
+                                                     long long chunks, long long passes, long long kpass,
+                                                     double* __restrict__ acc1, double* __restrict__ acc2,
+                                                     unsigned* __restrict__ nanc) {
   typedef typename BitsOf<V>::type B;
   __shared__ BigStage<B, RB> st;
-  const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
+  // CTA = (row block, label pass, chunk): a pass reduces the labels [klo, khi) only, so
+  // the accumulators it touches stay within the L2 budget
+  const long long rp = blockIdx.x / chunks, chunk = blockIdx.x - rp * chunks;
+  const long long rb = rp / passes, pass = rp - rb * passes;
+  const long long klo = pass * kpass, khi = min(K, klo + kpass);
   const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
   const int r = (threadIdx.x & 31) % RB;
   const bool live = rb * RB + r < rows;
@@ -794,7 +846,7 @@ __global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ va
 #pragma unroll
                         for (int e = 0; e < kBigT; ++e) {
                           const long long l = el[e];
-                          if (!live || l < 0 || l >= K) continue;
+                          if (!live || l < klo || l >= khi) continue;
                           const long long a = off + l * RB;
                           if (nan_bits(ev[e])) {
                             if (Need<F>::cnt) red_add_hint(&nanc[a], 1u, keep);
@@ -1090,7 +1142,8 @@ __global__ void fold_sel_kernel(const SelPart* __restrict__ parts, const V* __re
 struct FastPlan {
   int strategy;  // 0 tiny, 1 medium, 2 large
   long long chunks, chunk_len;  // large: chunks per row block
-  int rb;                       // large: rows per block (1, 4 or 8)
+  int rb;                       // large: rows per block (1, 2, 4, 8 or 16)
+  long long passes, kpass;      // large moments: label passes, labels per pass
   long long blocks;             // large: row blocks
 };
 
@@ -1138,8 +1191,19 @@ inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
   }
   p.rb = 1;
   p.blocks = rows;
+  p.passes = 1;
+  p.kpass = K;
   if (p.strategy == 2) {
     p.rb = big_rows_per_block(f, rows, K);
+    // moments: where the budget leaves fewer than 4 rows per block, 4 rows (a full
+    // 32-byte sector of float64 accumulators per label) in two passes over half the
+    // labels each beat fewer rows in one pass (half the L2 sector reductions, the
+    // values read twice)
+    if (is_moments(f) && p.rb < 4 && rows >= 4 && big_rows_per_block(f, rows, (K + 1) / 2) >= 4) {
+      p.rb = 4;
+      p.passes = 2;
+      p.kpass = (K + 1) / 2;
+    }
     p.blocks = (rows + p.rb - 1) / p.rb;
   }
   // large: CTAs per row block (four per SM); tiny / medium: CTAs per call, four
@@ -1212,11 +1276,18 @@ int launch_big_mom(const V* values, const L* labels, O* out, long long rows, lon
   if (Need<F>::cnt) {
     cudaMemsetAsync(nanc, 0, static_cast<size_t>(slots) * 4, s);
     cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
-    row_hist_kernel<L><<<fin_grid(max(m, kRcpN + 1)), FT, 0, s>>>(labels, m, K, hist, rcp);
+    if (K <= kHistSmem) {
+      auto hk = row_hist_kernel<L, true>;
+      set_smem(hk, static_cast<size_t>(K) * 4);
+      const int grid = static_cast<int>(max(1ll, min(static_cast<long long>(num_sms()) * 2, (m + FT * 64 - 1) / (FT * 64))));
+      hk<<<grid, FT, static_cast<size_t>(K) * 4, s>>>(labels, m, K, hist, rcp);
+    } else {
+      row_hist_kernel<L, false><<<fin_grid(max(m, kRcpN + 1)), FT, 0, s>>>(labels, m, K, hist, rcp);
+    }
     ++launches;
   }
-  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
-                                                                                   p.chunks, acc1, acc2, nanc);
+  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.passes * p.chunks), FT, 0, s>>>(
+      values, labels, rows, m, K, p.chunk_len, p.chunks, p.passes, p.kpass, acc1, acc2, nanc);
   big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
   return launches + 2;
 }
@@ -1247,7 +1318,7 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   if (!ws || ws_bytes < fast_bytes(F, rows, m, K)) return kWorkspaceTooSmall;
   unsigned char* cur = static_cast<unsigned char*>(ws);
   const long long nctas = rows * p.chunks;
-  if ((p.strategy < 2 ? nctas : p.blocks * p.chunks) > 0x7fffffffll) return kUnsupported;
+  if ((p.strategy < 2 ? nctas : p.blocks * p.passes * p.chunks) > 0x7fffffffll) return kUnsupported;
   // the float64 reductions of the large path are not reproducible bit for bit
   if (p.strategy == 2 && (Need<F>::s1 || Need<F>::s2) && deterministic_mode()) return kUnsupported;
   int launches = 0;
@@ -1265,7 +1336,7 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
                                                      d1, d2, parts);
       fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
-      launches = 2;
+      launches += 2;
     } else if (p.strategy == 1) {
       MomPart* parts = carve<MomPart>(cur, rows * p.chunks * K);
       unsigned* hist = carve<unsigned>(cur, p.chunks * K);
@@ -1284,8 +1355,8 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       launches += 2;
     } else {
       switch (p.rb) {
-        case 16: launches += launch_big_mom<F, V, L, O, 16>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
         case 8: launches += launch_big_mom<F, V, L, O, 8>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
+        case 16: launches += launch_big_mom<F, V, L, O, 16>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
         case 4: launches += launch_big_mom<F, V, L, O, 4>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
         case 2: launches += launch_big_mom<F, V, L, O, 2>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
         default: launches += launch_big_mom<F, V, L, O, 1>(values, labels, out, rows, m, K, ddof, p, cur, s); break;
@@ -1312,8 +1383,8 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
       launches = 2;
     } else {
       switch (p.rb) {
-        case 16: launches = launch_big_sel<F, V, L, O, 16>(values, labels, out, rows, m, K, p, cur, s); break;
         case 8: launches = launch_big_sel<F, V, L, O, 8>(values, labels, out, rows, m, K, p, cur, s); break;
+        case 16: launches = launch_big_sel<F, V, L, O, 16>(values, labels, out, rows, m, K, p, cur, s); break;
         case 4: launches = launch_big_sel<F, V, L, O, 4>(values, labels, out, rows, m, K, p, cur, s); break;
         case 2: launches = launch_big_sel<F, V, L, O, 2>(values, labels, out, rows, m, K, p, cur, s); break;
         default: launches = launch_big_sel<F, V, L, O, 1>(values, labels, out, rows, m, K, p, cur, s); break;
