@@ -405,8 +405,15 @@ NBG_DEVICE int block_max(int v, int* buf) {  // result valid in every thread; bu
   return r;
 }
 
+// CTAs per SM the kernels are compiled for: three for the single-input statistics, two
+// for covariance / correlation (five 128-bit sums)
+template <int OP>
+struct MoveOcc {
+  static constexpr int value = Traits<OP>::TWO ? 2 : 3;
+};
+
 template <int OP, typename T, bool C>
-__global__ void __launch_bounds__(NT, 2) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
+__global__ void __launch_bounds__(NT, MoveOcc<OP>::value) move_kernel(const T* __restrict__ a, const T* __restrict__ b,
                                                      T* __restrict__ out, Layout lay, long long window,
                                                      long long min_count, long long chunk_len,
                                                      const double* __restrict__ rcp, long long rcp_n,
@@ -644,9 +651,16 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
       sc.rcp, rcp_n, sc.first_bad, rows);
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
   auto kern = move_kernel<OP, T, C>;
-  if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  kern<<<layout_grid(grid_items, 4), NT, smem, stream>>>(a, b, out, lay, window, min_count, len, sc.rcp, rcp_n,
-                                                         sc.first_bad);
+  // the persistent grid: as many CTAs as can be resident at once (a CTA beyond that
+  // would wait for a slot and run as a tail)
+  static const int per_sm = [&] {
+    if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    int r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, NT, smem) != cudaSuccess || r < 1) r = 2;
+    return r;
+  }();
+  kern<<<layout_grid(grid_items, per_sm), NT, smem, stream>>>(a, b, out, lay, window, min_count, len, sc.rcp, rcp_n,
+                                                              sc.first_bad);
   move_poison_kernel<T, Traits<OP>::VARLIKE><<<static_cast<int>(std::min<long long>(rows, 4096)), 256, 0, stream>>>(
       out, lay, window, sc.first_bad);
   note_launches(launches);
