@@ -826,16 +826,11 @@ NBG_DEVICE long long big_col(long long cbase, int e) {
 template <int F, typename V, typename L, int RB>
 __global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                      long long rows, long long m, long long K, long long chunk_len,
-                                                     long long chunks, long long passes, long long kpass,
-                                                     double* __restrict__ acc1, double* __restrict__ acc2,
-                                                     unsigned* __restrict__ nanc) {
+                                                     long long chunks, double* __restrict__ acc1,
+                                                     double* __restrict__ acc2, unsigned* __restrict__ nanc) {
   typedef typename BitsOf<V>::type B;
   __shared__ BigStage<B, RB> st;
-  // CTA = (row block, label pass, chunk): a pass reduces the labels [klo, khi) only, so
-  // the accumulators it touches stay within the L2 budget
-  const long long rp = blockIdx.x / chunks, chunk = blockIdx.x - rp * chunks;
-  const long long rb = rp / passes, pass = rp - rb * passes;
-  const long long klo = pass * kpass, khi = min(K, klo + kpass);
+  const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
   const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
   const int r = (threadIdx.x & 31) % RB;
   const bool live = rb * RB + r < rows;
@@ -846,7 +841,7 @@ __global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ va
 #pragma unroll
                         for (int e = 0; e < kBigT; ++e) {
                           const long long l = el[e];
-                          if (!live || l < klo || l >= khi) continue;
+                          if (!live || l < 0 || l >= K) continue;
                           const long long a = off + l * RB;
                           if (nan_bits(ev[e])) {
                             if (Need<F>::cnt) red_add_hint(&nanc[a], 1u, keep);
@@ -1143,7 +1138,6 @@ struct FastPlan {
   int strategy;  // 0 tiny, 1 medium, 2 large
   long long chunks, chunk_len;  // large: chunks per row block
   int rb;                       // large: rows per block (1, 2, 4, 8 or 16)
-  long long passes, kpass;      // large moments: label passes, labels per pass
   long long blocks;             // large: row blocks
 };
 
@@ -1191,19 +1185,8 @@ inline FastPlan fast_plan(int f, long long rows, long long m, long long K) {
   }
   p.rb = 1;
   p.blocks = rows;
-  p.passes = 1;
-  p.kpass = K;
   if (p.strategy == 2) {
     p.rb = big_rows_per_block(f, rows, K);
-    // moments: where the budget leaves fewer than 4 rows per block, 4 rows (a full
-    // 32-byte sector of float64 accumulators per label) in two passes over half the
-    // labels each beat fewer rows in one pass (half the L2 sector reductions, the
-    // values read twice)
-    if (is_moments(f) && p.rb < 4 && rows >= 4 && big_rows_per_block(f, rows, (K + 1) / 2) >= 4) {
-      p.rb = 4;
-      p.passes = 2;
-      p.kpass = (K + 1) / 2;
-    }
     p.blocks = (rows + p.rb - 1) / p.rb;
   }
   // large: CTAs per row block (four per SM); tiny / medium: CTAs per call, four
@@ -1286,8 +1269,8 @@ int launch_big_mom(const V* values, const L* labels, O* out, long long rows, lon
     }
     ++launches;
   }
-  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.passes * p.chunks), FT, 0, s>>>(
-      values, labels, rows, m, K, p.chunk_len, p.chunks, p.passes, p.kpass, acc1, acc2, nanc);
+  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
+                                                                                   p.chunks, acc1, acc2, nanc);
   big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
   return launches + 2;
 }
@@ -1318,7 +1301,7 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   if (!ws || ws_bytes < fast_bytes(F, rows, m, K)) return kWorkspaceTooSmall;
   unsigned char* cur = static_cast<unsigned char*>(ws);
   const long long nctas = rows * p.chunks;
-  if ((p.strategy < 2 ? nctas : p.blocks * p.passes * p.chunks) > 0x7fffffffll) return kUnsupported;
+  if ((p.strategy < 2 ? nctas : p.blocks * p.chunks) > 0x7fffffffll) return kUnsupported;
   // the float64 reductions of the large path are not reproducible bit for bit
   if (p.strategy == 2 && (Need<F>::s1 || Need<F>::s2) && deterministic_mode()) return kUnsupported;
   int launches = 0;
