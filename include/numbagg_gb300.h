@@ -277,6 +277,51 @@ NBG_DECL_MATRIX(move_covmatrix, float, f32)
 NBG_DECL_MATRIX(move_corrmatrix, double, f64)
 NBG_DECL_MATRIX(move_corrmatrix, float, f32)
 
+/* ---- static aggregations over the last axis ----------------------------------------
+ * Replace numbagg/funcs.py:23-159 (ndaggregate: allnan, anynan, nancount, nansum,
+ * nanmean, nanvar, nanstd) and :162-242 (ndreduce: nanargmax, nanargmin, nanmax,
+ * nanmin).  a is a C-contiguous (rows, m) view whose last axis holds the reduced axes
+ * (moved last and flattened, numbagg/utils.py:20-32); out has rows elements:
+ *   allnan / anynan   -> unsigned char (0 / 1)
+ *   nancount          -> long long
+ *   nanargmax / min   -> long long, the first extreme column; -1 marks a row whose
+ *                        elements are all NaN (numbagg raises "All-NaN slice encountered")
+ *   the others        -> the input's type (nanmean / nanvar / nanstd: float64, float32;
+ *                        integer nansum wraps like the reference's integer loop)
+ * nanvar / nanstd take ddof (NaN unless count > ddof and count > 0).  nanmax / nanmin / nanarg*
+ * with m == 0 return NBG_INVALID_ARGUMENT (numbagg raises on an empty reduction).
+ * ws: nbg_aggregate_workspace_bytes(rows, m) bytes of scratch, no initialisation. */
+NBG_API size_t nbg_aggregate_workspace_bytes(long long rows, long long m);
+#define NBG_DECL_AGG(NAME, T, O, SFX) \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, O* out, long long rows, long long m, void* ws, size_t ws_bytes, void* stream);
+#define NBG_DECL_AGG_DDOF(NAME, T, SFX)                                                                      \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long m, long long ddof, void* ws, \
+                                 size_t ws_bytes, void* stream);
+#define NBG_DECL_AGG_ALL(NAME, O)          \
+  NBG_DECL_AGG(NAME, double, O, f64)       \
+  NBG_DECL_AGG(NAME, float, O, f32)        \
+  NBG_DECL_AGG(NAME, int, O, i32)          \
+  NBG_DECL_AGG(NAME, long long, O, i64)
+#define NBG_DECL_AGG_SAME(NAME)                  \
+  NBG_DECL_AGG(NAME, double, double, f64)        \
+  NBG_DECL_AGG(NAME, float, float, f32)          \
+  NBG_DECL_AGG(NAME, int, int, i32)              \
+  NBG_DECL_AGG(NAME, long long, long long, i64)
+NBG_DECL_AGG_ALL(allnan, unsigned char)
+NBG_DECL_AGG_ALL(anynan, unsigned char)
+NBG_DECL_AGG_ALL(nancount, long long)
+NBG_DECL_AGG_SAME(nansum)
+NBG_DECL_AGG(nanmean, double, double, f64)
+NBG_DECL_AGG(nanmean, float, float, f32)
+NBG_DECL_AGG_DDOF(nanvar, double, f64)
+NBG_DECL_AGG_DDOF(nanvar, float, f32)
+NBG_DECL_AGG_DDOF(nanstd, double, f64)
+NBG_DECL_AGG_DDOF(nanstd, float, f32)
+NBG_DECL_AGG_SAME(nanmax)
+NBG_DECL_AGG_SAME(nanmin)
+NBG_DECL_AGG_ALL(nanargmax, long long)
+NBG_DECL_AGG_ALL(nanargmin, long long)
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,12 +1,26 @@
 """numbagg_gb300: numbagg's scan and reduction hot path on a GB300 GPU.
 
 Drop-in replacements, same names and keywords, for numbagg's moving-window,
-exponentially weighted, fill and labelled-reduction functions.  Inputs may be torch
-CUDA tensors (results stay on the device) or numpy arrays / CPU tensors (copied to
-the current CUDA device and back).  The compute is hand-written sm_103a CUDA behind
+exponentially weighted, fill, labelled-reduction and static aggregation functions.
+Inputs may be torch CUDA tensors (results stay on the device) or numpy arrays / CPU
+tensors (copied to the current CUDA device and back).  The compute is hand-written sm_103a CUDA behind
 a C ABI (``include/numbagg_gb300.h``); there is no CPU fallback.
 """
 
+from .aggregate import (
+    allnan,
+    anynan,
+    count,
+    nanargmax,
+    nanargmin,
+    nancount,
+    nanmax,
+    nanmean,
+    nanmin,
+    nanstd,
+    nansum,
+    nanvar,
+)
 from .funcs import bfill, ffill
 from .grouped import (
     group_nanall,
@@ -40,7 +54,22 @@ from . import ragged  # noqa: E402  (ragged batches: an extension)
 
 __version__ = "1.0.0"
 
-# category lists, as numbagg/__init__.py:64-127 (restricted to this package's path)
+# category lists, as numbagg/__init__.py:64-127 (restricted to this package's path;
+# nanmedian / nanquantile and the static / EWM matrices are not built)
+AGGREGATION_FUNCS = [
+    allnan,
+    anynan,
+    count,
+    nanargmax,
+    nanargmin,
+    nancount,
+    nanmax,
+    nanmean,
+    nanmin,
+    nanstd,
+    nansum,
+    nanvar,
+]
 GROUPED_FUNCS = [
     group_nanall,
     group_nanany,
@@ -71,11 +100,15 @@ MOVE_FUNCS = [move_corr, move_cov, move_mean, move_corrmatrix, move_covmatrix, m
 OTHER_FUNCS = [bfill, ffill]
 
 __all__ = [
+    "AGGREGATION_FUNCS",
     "GROUPED_FUNCS",
     "MOVE_EXP_FUNCS",
     "MOVE_FUNCS",
     "OTHER_FUNCS",
+    "allnan",
+    "anynan",
     "bfill",
+    "count",
     "ffill",
     "group_nanall",
     "group_nanany",
@@ -107,4 +140,13 @@ __all__ = [
     "move_std",
     "move_sum",
     "move_var",
+    "nanargmax",
+    "nanargmin",
+    "nancount",
+    "nanmax",
+    "nanmean",
+    "nanmin",
+    "nanstd",
+    "nansum",
+    "nanvar",
 ]

@@ -99,6 +99,15 @@ def _declare(lib: ctypes.CDLL) -> None:
     for dt in ("f64", "f32", "i32", "i64"):
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+    # static aggregations over the last axis
+    sig("nbg_aggregate_workspace_bytes", c_sz, c_ll, c_ll)
+    for dt in ("f64", "f32", "i32", "i64"):
+        for f in ("allnan", "anynan", "nancount", "nansum", "nanmax", "nanmin", "nanargmax", "nanargmin"):
+            sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
+    for dt in ("f64", "f32"):
+        sig(f"nbg_nanmean_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
+        for f in ("nanvar", "nanstd"):
+            sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
     for name in GROUP_FUNC_IDS:
         vdts = ("f64", "f32") if name in ("nanmean", "nanvar", "nanstd") else ("f64", "f32", "i32", "i64")
         for vd in vdts:

@@ -250,3 +250,88 @@ __all__ = [
     "move_exp",
     "move_matrix",
 ]
+
+
+# ---- static aggregations (numbagg/funcs.py:23-242), restated in numpy --------------------
+AGG_INT_FLOAT_LOOPS = (np.int32, np.int64, np.float32, np.float64)
+AGG_FLOAT_LOOPS = (np.float32, np.float64)
+
+
+def _seq_sum(x: np.ndarray, dtype) -> np.ndarray:
+    """Sequential left-to-right sum along the last axis in `dtype` (a numba loop's
+    order): the last element of the running sum."""
+    if x.shape[-1] == 0:
+        return np.zeros(x.shape[:-1], dtype=dtype)
+    return np.add.accumulate(x.astype(dtype), axis=-1, dtype=dtype)[..., -1]
+
+
+def aggregate(name, a, *, axis=None, ddof=1, ext=False):
+    """numbagg.<name> for the static aggregations, restated from numbagg/funcs.py:23-242
+    with the axis handling of ndaggregate / ndreduce (numbagg/decorators.py:231-255,
+    :1002-1028; numbagg/utils.py:20-32).  The loop dtype is the first of the reference's
+    signatures the input casts to safely.  ext=True sums in long double (the
+    accuracy yardstick); otherwise sums run left to right in the reference's
+    accumulator dtype."""
+    a = np.asarray(a)
+    loops = AGG_FLOAT_LOOPS if name in ("nanmean", "nanvar", "nanstd") else AGG_INT_FLOAT_LOOPS
+    loop = next((lp for lp in loops if np.can_cast(a.dtype, lp, casting="safe")), None)
+    if loop is None:
+        raise TypeError(f"ufunc '{name}' not supported for the input types {a.dtype}")
+    a = a.astype(loop)
+    if a.ndim == 0:
+        a = a.reshape(1)
+    if axis is None:
+        axes = tuple(range(a.ndim))
+    elif isinstance(axis, tuple):
+        axes = tuple(ax % a.ndim for ax in axis)
+    else:
+        axes = (axis % a.ndim,)
+    moved = np.moveaxis(a, axes, range(a.ndim - len(axes), a.ndim))
+    out_shape = moved.shape[: a.ndim - len(axes)]
+    m = int(np.prod(moved.shape[a.ndim - len(axes) :], dtype=np.int64))
+    x = np.ascontiguousarray(moved).reshape(out_shape + (m,))
+    is_float = np.issubdtype(loop, np.floating)
+    nan = np.isnan(x) if is_float else np.zeros(x.shape, dtype=bool)
+    cnt = (~nan).sum(axis=-1).astype(np.int64)
+    acc = np.longdouble if ext else np.float64
+    zeroed = np.where(nan, 0, x)
+    if name == "allnan":
+        return nan.all(axis=-1)
+    if name == "anynan":
+        return nan.any(axis=-1)
+    if name == "nancount":
+        return cnt
+    if name == "nansum":
+        if not is_float:
+            return zeroed.sum(axis=-1, dtype=loop)  # wraps like the integer loop
+        return _seq_sum(zeroed, acc if ext else loop).astype(loop)  # numbagg/funcs.py:79-84
+    if name == "nanmean":
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return (_seq_sum(zeroed, acc) / cnt).astype(loop)  # :93-103
+    if name in ("nanvar", "nanstd"):  # two passes, :113-133 / :143-159
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mean = _seq_sum(zeroed, acc) / cnt
+            dev = np.where(nan, 0, x.astype(acc) - mean[..., None])
+            ss = _seq_sum(dev * dev, acc)
+            v = ss / (cnt - ddof)
+            v = np.where((cnt > ddof) & (cnt > 0), v, np.nan)
+            if name == "nanstd":
+                v = np.sqrt(v)
+        return v.astype(loop)
+    if name in ("nanmax", "nanmin"):  # :207-242
+        if m == 0 and x.size == 0 and int(np.prod(out_shape)) > 0:
+            op = "fmax" if name == "nanmax" else "fmin"
+            raise ValueError(f"zero-size array to reduction operation {op} which has no identity")
+        if not is_float:
+            return x.max(axis=-1) if name == "nanmax" else x.min(axis=-1)
+        fill = -np.inf if name == "nanmax" else np.inf
+        r = np.where(nan, fill, x)
+        r = r.max(axis=-1) if name == "nanmax" else r.min(axis=-1)
+        return np.where(cnt > 0, r, np.nan).astype(loop)
+    if name in ("nanargmax", "nanargmin"):  # :167-199: the first extreme, raising on all-NaN
+        if int(np.prod(out_shape)) > 0 and (m == 0 or (cnt == 0).any()):
+            raise ValueError("All-NaN slice encountered")
+        fill = -np.inf if name == "nanargmax" else np.inf
+        r = np.where(nan, fill, x) if is_float else x
+        return (r.argmax(axis=-1) if name == "nanargmax" else r.argmin(axis=-1)).astype(np.int64)
+    raise ValueError(f"unknown aggregation {name}")
