@@ -61,11 +61,11 @@ def parse_args(argv=None):
     p.add_argument("--only", default=None, help="regex: time only the calls whose key matches (profiling)")
     p.add_argument(
         "--suite",
-        choices=("group_fill", "scan", "ragged", "link"),
+        choices=("group_fill", "scan", "ragged", "link", "aggregate"),
         default="group_fill",
         help="group_fill: the headline workload; scan: the moving-window, EWM and matrix shapes; "
         "ragged: the batched mix of series of uneven length; link: pinned host<->device copy "
-        "bandwidth (the bound of the end-to-end number)",
+        "bandwidth (the bound of the end-to-end number); aggregate: the static aggregations",
     )
     p.add_argument("--ragged-series", type=int, default=20_000, help="series in the ragged batch")
     return p.parse_args(argv)
@@ -791,6 +791,66 @@ def run_ragged_suite(args):
     return 0
 
 
+def run_aggregate_suite(args):
+    """The static aggregations over the last axis of the headline's values: float64
+    64 x cols, N(0,1) with 5% NaN; 8 algorithmic bytes per element (the reads)."""
+    import torch
+
+    import numbagg_gb300 as nb
+    from numbagg_gb300 import _lib
+
+    world, rank, local = dist_env()
+    device = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+    g = torch.Generator(device=device)
+    g.manual_seed(1)
+    values = torch.randn((ROWS, args.cols), generator=g, dtype=torch.float64, device=device)
+    values[torch.rand((ROWS, args.cols), generator=g, device=device) < NAN_P] = float("nan")
+    calls = {
+        "nansum": lambda: nb.nansum(values, axis=-1),
+        "nanmean": lambda: nb.nanmean(values, axis=-1),
+        "nanvar": lambda: nb.nanvar(values, axis=-1),
+        "nancount": lambda: nb.nancount(values, axis=-1),
+        "nanmax": lambda: nb.nanmax(values, axis=-1),
+        "nanargmax": lambda: nb.nanargmax(values, axis=-1),
+        "anynan": lambda: nb.anynan(values, axis=-1),
+        "nansum_all_axes": lambda: nb.nansum(values),
+    }
+    peak, peak_kind = measured_peak()
+    stream = torch.cuda.current_stream(device)
+    nbytes = 8 * values.numel()
+    res = {}
+    launches0 = _lib.launch_count()
+    for key, fn in calls.items():
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = nbytes / (ms / 1e3) / 1e9
+        res[key] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    line = {
+        "suite": "aggregate",
+        "metric": "HBM GB/s of the static aggregations (8 bytes read per element)",
+        "config": {"values": f"float64 {ROWS} x {args.cols}, N(0,1), {NAN_P:.0%} NaN", "axis": -1},
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "per_func": res,
+        "note": "nanargmax synchronises once per call to check for all-NaN slices; nanvar is two passes",
+        "gpu_launches": int(_lib.launch_count() - launches0),
+        "steps": args.steps,
+        "warmup": args.warmup,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_link_suite(args):
     """Pinned host <-> device copy bandwidth through the copy engines (4 GiB per copy):
     each direction alone, and both at once on two streams.  The end-to-end step moves
@@ -863,6 +923,8 @@ def main(argv=None):
         return run_ragged_suite(args)
     if args.suite == "link":
         return run_link_suite(args)
+    if args.suite == "aggregate":
+        return run_aggregate_suite(args)
     return run_ours(args)
 
 
