@@ -17,9 +17,11 @@ run with that same rewrite applied (see ``_StaticPower``).
 
 Usage (needs a numbagg source tree; the GPU machine does not):
 
-    python tests/golden/make_golden.py /path/to/numbagg-source
+    python tests/golden/make_golden.py [--aggregates-only] /path/to/numbagg-source
 
-The output file is small and committed; tests read it without numbagg.
+It writes ``reference_vectors.npz`` (the scan, fill, grouped and matrix kernels) and
+``aggregate_vectors.npz`` (the static aggregations); ``--aggregates-only`` writes the
+second alone.  The files are small and committed; tests read them without numbagg.
 """
 
 from __future__ import annotations
@@ -325,17 +327,89 @@ def generate(src: str) -> dict[str, np.ndarray]:
     return vec
 
 
-def main() -> None:
-    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NUMBAGG_SRC", "")
-    if not src or not os.path.isdir(os.path.join(src, "numbagg")):
-        sys.exit("usage: make_golden.py <numbagg source tree>")
-    vec = generate(src)
+AGG_OUT = os.path.join(HERE, "aggregate_vectors.npz")
+
+
+def generate_aggregates(src: str) -> dict[str, np.ndarray]:
+    """The static aggregations (numbagg/funcs.py:23-242) run row by row through their
+    own kernel bodies: ndaggregate bodies take (row, [ddof,] out[1]), ndreduce bodies
+    take a row and return a scalar.  float32 rows run unchanged where numba and NumPy
+    type the locals alike (the float32 nansum accumulator, the extremes, the counts) and
+    widened to float64 where numba's locals are float64 (nanmean, nanvar, nanstd)."""
+    nb = _import_numbagg(src)
+    vec: dict[str, np.ndarray] = {}
+    f64 = _fixture_array((5, 37), seed=9)
+    f64[1, 3] = np.inf
+    f64[2, 5] = -np.inf
+    f64[3, :] = np.nan  # an all-NaN row (the arg functions use the other rows)
+    shifted = 1e6 + np.random.RandomState(10).randn(3, 41)
+    shifted[0, ::7] = np.nan
+    ints = np.random.RandomState(11).randint(-1000, 1000, size=(4, 29))
+    big = np.full((2, 8), 2**30)
+    inputs = {
+        "f64": f64,
+        "f64shift": shifted,
+        "f32": f64.astype(np.float32),
+        "i32": ints.astype(np.int32),
+        "i64": ints.astype(np.int64),
+        "i32big": big.astype(np.int32),
+    }
+    for key, a in inputs.items():
+        vec[f"agg_in|{key}"] = a
+    widen = {"nanmean", "nanvar", "nanstd"}
+    for name in ("allnan", "anynan", "nancount", "nansum", "nanmean", "nanvar", "nanstd"):
+        body = _as_compiled(getattr(nb, name).func)
+        for key, a in inputs.items():
+            if name in widen and a.dtype.kind == "i":
+                continue
+            for ddof in ((0, 1, 3) if name in ("nanvar", "nanstd") else (None,)):
+                res = []
+                for r in range(a.shape[0]):
+                    row = a[r].astype(np.float64) if (name in widen and a.dtype == np.float32) else a[r]
+                    if name in ("allnan", "anynan"):
+                        out = np.empty(1, dtype=np.bool_)
+                    elif name == "nancount":
+                        out = np.empty(1, dtype=np.int64)
+                    else:
+                        out = np.empty(1, dtype=row.dtype)
+                    with np.errstate(all="ignore"):
+                        if ddof is None:
+                            body(row, out)
+                        else:
+                            body(row, ddof, out)
+                    res.append(out[0])
+                dtype = a.dtype if name in ("nansum", "nanmean", "nanvar", "nanstd") else None
+                vec[f"agg|{name}|{key}|{ddof}"] = np.array(res, dtype=dtype)
+    for name in ("nanmax", "nanmin", "nanargmax", "nanargmin"):
+        body = _as_compiled(getattr(nb, name).func)
+        for key, a in inputs.items():
+            rows = [r for r in range(a.shape[0]) if not (a.dtype.kind == "f" and np.isnan(a[r]).all())]
+            if name in ("nanmax", "nanmin"):
+                rows = list(range(a.shape[0]))
+            with np.errstate(all="ignore"):
+                res = [body(a[r]) for r in rows]
+            vec[f"agg|{name}|{key}|rows"] = np.array(rows, dtype=np.int64)
+            vec[f"agg|{name}|{key}|None"] = np.array(res, dtype=np.int64 if "arg" in name else a.dtype)
+    return vec
+
+
+def _write(vec: dict[str, np.ndarray], path: str) -> None:
     keys = sorted(vec)
     with tempfile.NamedTemporaryFile(dir=HERE, suffix=".npz", delete=False) as fh:
         np.savez_compressed(fh, **{k: vec[k] for k in keys})
         tmp = fh.name
-    os.replace(tmp, OUT)
-    print(f"wrote {len(keys)} arrays to {OUT} ({os.path.getsize(OUT)} bytes)")
+    os.replace(tmp, path)
+    print(f"wrote {len(keys)} arrays to {path} ({os.path.getsize(path)} bytes)")
+
+
+def main() -> None:
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    src = args[0] if args else os.environ.get("NUMBAGG_SRC", "")
+    if not src or not os.path.isdir(os.path.join(src, "numbagg")):
+        sys.exit("usage: make_golden.py [--aggregates-only] <numbagg source tree>")
+    if "--aggregates-only" not in sys.argv:
+        _write(generate(src), OUT)
+    _write(generate_aggregates(src), AGG_OUT)
 
 
 if __name__ == "__main__":
