@@ -1,0 +1,112 @@
+"""Host-side logic that needs no GPU: the ragged module's input checks and its
+autotuning cache, and the benchmark's byte accounting and peak / traffic lookups."""
+
+import importlib.util
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from numbagg_gb300 import ragged
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("bench_module", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+# ---- ragged -------------------------------------------------------------------------------
+
+
+def test_ragged_rejects_host_tensors_and_bad_dtypes():
+    values = torch.zeros(10, dtype=torch.float64)
+    offsets = torch.tensor([0, 4, 10], dtype=torch.int64)
+    with pytest.raises(TypeError, match="values must be a 1-D float64 CUDA tensor"):
+        ragged.move_mean(values, offsets, window=3)
+    with pytest.raises(TypeError, match="values must be a 1-D float64 CUDA tensor"):
+        ragged.group_nansum(values.float(), torch.zeros(10, dtype=torch.int32), offsets, num_labels=2)
+
+
+def test_ragged_precision_keyword():
+    assert ragged._sfx("f64") == "f64"
+    assert ragged._sfx("fp32c") == "f64_fp32c"
+    with pytest.raises(ValueError, match="precision must be one of"):
+        ragged._sfx("fp16")
+
+
+def test_autotune_shape_buckets():
+    k = ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 20)
+    assert k == ragged._shape_key("move_mean", "f64", 30_000, 2_000_000_000, 20)  # same power-of-two buckets
+    assert k != ragged._shape_key("move_mean", "f64", 40_000, 2_000_000_000, 20)
+    assert k != ragged._shape_key("move_mean", "fp32c", 20_000, 1_830_000_000, 20)
+    assert k != ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 21)
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    path = tmp_path / "tune.json"
+    monkeypatch.setattr(ragged, "_CACHE_FILE", str(path))
+    monkeypatch.setattr(ragged, "_cache", {"move_mean|f64|s14|n30|w20": 32768})
+    ragged._save_cache()
+    assert json.loads(path.read_text()) == {"move_mean|f64|s14|n30|w20": 32768}
+    monkeypatch.setattr(ragged, "_cache", {})
+    ragged._load_cache()
+    assert ragged._cache == {"move_mean|f64|s14|n30|w20": 32768}
+    path.write_text("not json")
+    monkeypatch.setattr(ragged, "_cache", {})
+    ragged._load_cache()  # a corrupt file is ignored
+    assert ragged._cache == {}
+
+
+# ---- bench --------------------------------------------------------------------------------
+
+
+def test_bench_byte_accounting():
+    b = _bench()
+    rows, cols = 64, 1 << 20
+    calls = b.calls_and_bytes(rows, cols)
+    assert len(calls) == 19
+    keys = [c[0] for c in calls]
+    assert len(set(keys)) == 19
+    for key, (kind, f, arg), nbytes in calls:
+        if kind == "fill":
+            assert nbytes == 16 * rows * cols  # read + write
+        else:
+            assert nbytes == 8 * rows * cols + 4 * cols + 8 * rows * arg  # values + labels + output
+
+
+def test_bench_peak_and_traffic_lookups(tmp_path, monkeypatch):
+    b = _bench()
+    monkeypatch.setattr(b, "ROOT", str(tmp_path))
+    assert b.measured_peak() == (6800.0, "fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6781.8}))
+    assert b.measured_peak() == (6781.8, "measured")
+    assert b.traffic_for("group_nanvar_K1000000") is None
+    (tmp_path / "profiles").mkdir()
+    (tmp_path / "profiles" / "traffic.json").write_text(json.dumps({"group_nanvar_K1000000": 123}))
+    assert b.traffic_for("group_nanvar_K1000000") == 123
+
+
+def test_committed_traffic_covers_the_dominant_call():
+    with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+        data = json.load(fh)
+    assert isinstance(data.get("group_nanvar_K1000000"), int)
+    assert data["group_nanvar_K1000000"] > 9_169_043_456  # at least the algorithmic bytes
+
+
+def test_bench_cpu_sample_is_a_prefix_of_the_workload():
+    b = _bench()
+    rows, cols = 4, 4096
+    values = torch.arange(rows * cols, dtype=torch.float64).reshape(rows, cols)
+    labels = {K: torch.zeros(cols, dtype=torch.int32) for K in b.KS}
+    fill = values.clone()
+    v, lab, fl, sc = b.cpu_sample(values, labels, fill, cols)
+    assert sc <= cols
+    np.testing.assert_array_equal(np.asarray(v), values[:, :sc].numpy())
+    assert b.sample_bytes(rows, sc) > 0
+    assert str(sc) in b.sample_desc(rows, sc)
