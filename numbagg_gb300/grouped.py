@@ -161,8 +161,10 @@ def _make(name: str, doc_lines: str):
             return _group(name, values, labels, ddof=ddof, num_labels=num_labels, axis=axis)
 
     else:
+        # numbagg accepts ddof for every grouped function and ignores it where the
+        # function has none (groupndreduce.__call__, numbagg/decorators.py:558-674)
 
-        def f(values, labels, *, num_labels=None, axis=None):
+        def f(values, labels, *, ddof=1, num_labels=None, axis=None):
             return _group(name, values, labels, num_labels=num_labels, axis=axis)
 
     f.__name__ = f.__qualname__ = f"group_{name}"
