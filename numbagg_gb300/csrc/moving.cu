@@ -651,10 +651,11 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
       sc.rcp, rcp_n, sc.first_bad, rows);
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
   auto kern = move_kernel<OP, T, C>;
+  // the shared-memory opt-in is per device, so it is set on every call
+  if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   // the persistent grid: as many CTAs as can be resident at once (a CTA beyond that
   // would wait for a slot and run as a tail)
   static const int per_sm = [&] {
-    if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int r = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, NT, smem) != cudaSuccess || r < 1) r = 2;
     return r;
