@@ -76,3 +76,12 @@ def test_workspace_queries(lib):
     assert lib.nbg_fill_workspace_bytes(64, 1 << 24) > lib.nbg_fill_workspace_bytes(64, 1 << 10)
     assert lib.nbg_group_workspace_bytes(0, 4, 1000, 16) >= 4 * 16 * 24
     assert lib.nbg_group_workspace_bytes(99, 4, 1000, 16) == 0
+
+
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])
+def test_header_compiles_standalone(lang, std):
+    """A C or C++ host (or a cgo / JNI stub) includes the header with nothing else."""
+    cc = "gcc" if lang == "c" else "g++"
+    res = subprocess.run([cc, "-fsyntax-only", std, "-Wall", "-Wextra", "-Werror", "-x", lang, HEADER],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
