@@ -205,13 +205,19 @@ NBG_DECL_FILL(long long, i64)
  * library's device image (every GPU that loads the library keeps it until the
  * process exits), so a call may cover at most that many tiles: rows x ceil(n / 4096)
  * tiles within nbg_ffill_noalloc_max_scratch_bytes(); larger problems return
- * NBG_TOO_LARGE without launching.  The first call on a device looks up and clears
- * the array on `stream`; make that first call before any stream capture.  All calls
- * on a device share the one array: calls that overlap on the GPU (different streams,
- * or concurrent threads) race and must be serialised by the caller. */
+ * NBG_TOO_LARGE without launching.  The array is zero when the library's device code
+ * loads and every launch leaves it in that state.  Each call looks up the array's
+ * address on the current device; the first call on a device may load the library's
+ * device code, so make it before any stream capture.  All calls on a device share
+ * the one array: calls that overlap on the GPU (different streams, or concurrent
+ * threads) race and must be serialised by the caller.
+ * nbg_ffill_noalloc_error reads and clears the array's error word (a look-back wait
+ * that ran out of its bound records NBG_LOOKBACK_TIMEOUT and the tile there, as in a
+ * workspace); it synchronises `stream`. */
 NBG_API size_t nbg_ffill_noalloc_max_scratch_bytes(void);
 NBG_API int nbg_ffill_f64_noalloc(const double* a, double* out, long long rows, long long n,
                                   long long limit, void* stream);
+NBG_API int nbg_ffill_noalloc_error(int* code, unsigned* tile, void* stream);
 
 /* ---- grouped reductions ----------------------------------------------------------------
  * Replaces the gufuncs built by groupndreduce (numbagg/decorators.py:490-674) from

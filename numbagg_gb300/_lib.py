@@ -64,6 +64,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     sig("nbg_fill_workspace_bytes", c_sz, c_ll, c_ll)
     sig("nbg_ffill_noalloc_max_scratch_bytes", c_sz)
     sig("nbg_ffill_f64_noalloc", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp)
+    sig("nbg_ffill_noalloc_error", c_i, ctypes.POINTER(c_i), ctypes.POINTER(ctypes.c_uint), c_vp)
     sig("nbg_group_workspace_bytes", c_sz, c_i, c_ll, c_ll, c_ll)
     for dt in ("f64", "f32"):
         for f in ("move_sum", "move_mean", "move_var", "move_std"):

@@ -18,8 +18,6 @@
 // copy through double.
 #include "nbg_common.cuh"
 
-#include <mutex>
-
 namespace nbg {
 namespace fill {
 
@@ -287,27 +285,20 @@ NBG_FILL_I(long long, i64)
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = static_cast<size_t>(4) << 20;  // 4 MiB per device
+// Zero when the module loads (PTX initialises .global variables without an initialiser
+// to zero), which is the state a look-back workspace must start in; every launch
+// leaves it that way again (the last CTA resets the counters), so no call clears it.
 __device__ __align__(256) unsigned char g_fill_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device.  The first call on a
-// device looks the address up and zero-fills the array on `stream` (the fill kernel
-// that follows on the same stream sees it cleared).  In host code the array's name
-// is only a host-side stand-in, never a device address.
-int noalloc_scratch(cudaStream_t stream, void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return kLaunchError;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_fill_noalloc_scratch) != cudaSuccess || !p) return kLaunchError;
-    if (cudaMemsetAsync(p, 0, kNoAllocScratchBytes, stream) != cudaSuccess) return kLaunchError;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+// Device address of the scratch array on the current device.  In host code the
+// array's name is only a host-side stand-in, never a device address, so every call
+// asks the runtime for the address on the device that is current.  The lookup
+// allocates nothing; doing it on every call (rather than caching it per device) keeps
+// a call after cudaDeviceReset from launching on the address of a module that is gone.
+int noalloc_scratch(void** out) {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_fill_noalloc_scratch) != cudaSuccess || !p) return kLaunchError;
+  *out = p;
   return kOk;
 }
 
@@ -324,11 +315,24 @@ int nbg_ffill_f64_noalloc(const double* a, double* out, long long rows, long lon
   if (!a || !out) return kInvalidArgument;
   const long long tpr = fill_tiles_per_row(n);
   if (workspace_bytes(rows * tpr) > kNoAllocScratchBytes) return kTooLarge;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
-  const int st = noalloc_scratch(s, &scratch);
+  const int st = noalloc_scratch(&scratch);
   if (st != kOk) return st;
-  return launch_fill<double, false>(a, out, rows, n, limit, scratch, kNoAllocScratchBytes, s);
+  return launch_fill<double, false>(a, out, rows, n, limit, scratch, kNoAllocScratchBytes,
+                                    static_cast<cudaStream_t>(stream));
+}
+
+// The error word of the fixed scratch: a look-back wait that ran out of its bound
+// during an earlier call records NBG_LOOKBACK_TIMEOUT there (and the tile), exactly as
+// it does in a caller's workspace, where nbg_workspace_error reads it.  Synchronises
+// `stream`, then clears the word.  Plain copies of 8 bytes to and from host memory;
+// nothing is allocated.
+int nbg_ffill_noalloc_error(int* code, unsigned* tile, void* stream) {
+  if (!code || !tile) return kInvalidArgument;
+  void* scratch = nullptr;
+  const int st = noalloc_scratch(&scratch);
+  if (st != kOk) return st;
+  return nbg_workspace_error(scratch, code, tile, stream);
 }
 
 }  // extern "C"

@@ -4,7 +4,9 @@
 // skipped (numbagg/grouped.py:14); a label >= K is skipped as well (numba would write
 // out of bounds there, so the reference leaves it undefined).
 //
-// Two strategies, picked on the host from K:
+// This file holds the integer sums, counts and sums of squares and every product,
+// any and all; float moments and every selection (argmax/argmin/max/min/first/last)
+// live in grouped_fast.cu.  Two strategies, picked on the host from K:
 //   * shared-memory bins (K * 24 B fits in shared memory): a CTA owns one column
 //     chunk of one row and accumulates into bins in shared memory, replicated per
 //     lane (no atomics) for tiny K, per warp for small K, or per CTA; at the end it
@@ -12,13 +14,6 @@
 //     chunks in chunk order and writes the output, so results repeat run to run.
 //   * global bins (large K, e.g. 10^6 labels): atomics into an accumulator in the
 //     workspace, then the same fold/finalise kernel with one chunk.
-//
-// Selection kernels keep numbagg's float64 running extreme with a strict comparison
-// (first index wins on ties, numbagg/grouped.py:62, :86, :221, :239).  Here every
-// element becomes an order key of its float64 value in which -0.0 == +0.0; a first
-// sweep takes the maximum key per bin and a second sweep the minimum column index
-// among the elements holding that key.  The (key, first index) pair is exactly the
-// sequential result, so argmax/argmin/max/min/first/last are bit-exact.
 //
 // Integer sums, products and sums of squares wrap modulo 2^64 and are truncated to
 // the output type, which equals numba's int64 arithmetic stored into the narrow

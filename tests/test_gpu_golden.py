@@ -151,8 +151,8 @@ def test_move_matrix_golden(golden, fname):
             scale = np.ones_like(want) if fname == "move_corrmatrix" else np.nanmax(np.abs(want)) * np.ones_like(want)
             assert_parity(got, want, ext, scale, F64_TOL, None, key)
         else:
-            # the reference accumulates float32 in float32; this implementation in
-            # float64, so the float32 reference carries the larger error
+            # both the reference and this implementation accumulate float32 input in
+            # float32, in different orders, so each carries float32 rounding error
             scale = np.ones_like(want) if fname == "move_corrmatrix" else np.nanmax(np.abs(want)) * np.ones_like(want)
             # a window holding <= 2 complete pairs has correlation +-1 exactly; the
             # float32-accumulated reference returns its rounding noise there

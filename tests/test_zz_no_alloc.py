@@ -9,11 +9,15 @@ the library's device image instead of a caller-provided workspace.
 
 The test calls it through the C ABI twice in a row on different inputs and checks
 each result against the ordinary entry point nbg_ffill_f64 (a fill only selects
-values, so the two must agree bit for bit), then checks that a problem larger than
-the fixed scratch is refused without a launch.  This file is named so that pytest
+values, so the two must agree bit for bit) and that no look-back wait gave up
+(nbg_ffill_noalloc_error reads (0, 0)).  It then checks that a problem larger than
+the fixed scratch is refused without a launch and that a call after the refusal
+still matches the ordinary entry point.  This file is named so that pytest
 collects it last; it passes both on its own in a fresh process and after the rest of
 the suite.
 """
+
+import ctypes
 
 import numpy as np
 import pytest
@@ -33,25 +37,36 @@ def _ffill_with_workspace(L, x, limit, stream):
     return out
 
 
-def test_noalloc_ffill_matches_workspace_entry_twice():
-    L = _lib.lib()
+def _noalloc_error(L, stream):
+    code, tile = ctypes.c_int(-1), ctypes.c_uint(12345)
+    assert L.nbg_ffill_noalloc_error(ctypes.byref(code), ctypes.byref(tile), stream) == 0
+    return code.value, tile.value
+
+
+def _check_against_workspace_entry(L, rng, rows, n, limit, what):
     dev = torch.device("cuda", 0)
     stream = _lib.stream_handle(dev)
+    x = rng.standard_normal((rows, n))
+    x[rng.random(x.shape) < 0.3] = np.nan
+    x[0, min(1000, n) : min(30_000, n)] = np.nan  # a NaN run across several tiles
+    xt = torch.from_numpy(x).to(dev)
+    out = torch.full_like(xt, 7.0)
+    status = L.nbg_ffill_f64_noalloc(xt.data_ptr(), out.data_ptr(), rows, n, limit, stream)
+    assert status == 0, _lib.STATUS.get(status)
+    want = _ffill_with_workspace(L, xt, limit, stream)
+    torch.cuda.synchronize()
+    got_np, want_np = out.cpu().numpy(), want.cpu().numpy()
+    assert np.array_equal(np.isnan(got_np), np.isnan(want_np)), f"{what}: NaN placement"
+    keep = ~np.isnan(want_np)
+    assert np.array_equal(got_np[keep], want_np[keep]), f"{what}: values"
+    assert _noalloc_error(L, stream) == (0, 0), f"{what}: a look-back wait gave up"
+
+
+def test_noalloc_ffill_matches_workspace_entry_twice():
+    L = _lib.lib()
     rng = np.random.default_rng(123)
     for call, (rows, n, limit) in enumerate([(7, 50_001, 3), (3, 200_000, 200_000)]):
-        x = rng.standard_normal((rows, n))
-        x[rng.random(x.shape) < 0.3] = np.nan
-        x[0, 1000:30_000] = np.nan  # a NaN run across several tiles
-        xt = torch.from_numpy(x).to(dev)
-        out = torch.full_like(xt, 7.0)
-        status = L.nbg_ffill_f64_noalloc(xt.data_ptr(), out.data_ptr(), rows, n, limit, stream)
-        assert status == 0, _lib.STATUS.get(status)
-        want = _ffill_with_workspace(L, xt, limit, stream)
-        torch.cuda.synchronize()
-        got_np, want_np = out.cpu().numpy(), want.cpu().numpy()
-        assert np.array_equal(np.isnan(got_np), np.isnan(want_np)), f"call {call}: NaN placement"
-        keep = ~np.isnan(want_np)
-        assert np.array_equal(got_np[keep], want_np[keep]), f"call {call}: values"
+        _check_against_workspace_entry(L, rng, rows, n, limit, f"call {call}")
 
 
 def test_noalloc_ffill_rejects_problems_beyond_its_scratch():
@@ -68,3 +83,5 @@ def test_noalloc_ffill_rejects_problems_beyond_its_scratch():
     status = L.nbg_ffill_f64_noalloc(x.data_ptr(), out.data_ptr(), rows, n, 5, _lib.stream_handle(dev))
     assert status == 6, _lib.STATUS.get(status)
     assert L.nbg_ffill_f64_noalloc(None, None, -1, 10, 1, None) == 1
+    # the refused calls touched nothing: the scratch still serves a call
+    _check_against_workspace_entry(L, np.random.default_rng(7), 5, 70_000, 10, "after the refusal")
