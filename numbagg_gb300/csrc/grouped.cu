@@ -6,7 +6,7 @@
 //
 // This file holds the integer sums, counts and sums of squares and every product,
 // any and all; float moments and every selection (argmax/argmin/max/min/first/last)
-// live in grouped_fast.cu.  Two strategies, picked on the host from K:
+// live in grouped_fast.cuh.  Two strategies, picked on the host from K:
 //   * shared-memory bins (K * 24 B fits in shared memory): a CTA owns one column
 //     chunk of one row and accumulates into bins in shared memory, replicated per
 //     lane (no atomics) for tiny K, per warp for small K, or per CTA; at the end it
@@ -304,7 +304,7 @@ size_t nbg_group_workspace_bytes(int func, long long rows, long long m, long lon
   NBG_GROUP_LABELS(NAME, FC, int, i32, int) \
   NBG_GROUP_LABELS(NAME, FC, long long, i64, long long)
 
-// float moments and all selections live in grouped_fast.cu
+// float moments and all selections live in grouped_fast.cuh (grouped_fast_*.cu)
 NBG_GROUP_INTONLY(nansum, kSum)
 NBG_GROUP_INTONLY(nancount, kCount)
 NBG_GROUP_INTONLY(nansum_of_squares, kSumSq)

@@ -1,4 +1,4 @@
-// Shared declarations of the labelled-reduction kernels (grouped.cu, grouped_fast.cu).
+// Shared declarations of the labelled-reduction kernels (grouped.cu, grouped_fast.cuh).
 #pragma once
 
 #include "nbg_common.cuh"
@@ -195,7 +195,7 @@ NBG_DEVICE O nan_of() {
   return sizeof(O) == 4 ? static_cast<O>(INT_MIN) : static_cast<O>(LLONG_MIN);
 }
 
-// scratch bytes of the fast paths (grouped_fast.cu); 0 for functions they do not serve
+// scratch bytes of the fast paths (grouped_fast.cuh); 0 for functions they do not serve
 size_t fast_bytes_query(int f, long long rows, long long m, long long K);
 
 inline int num_sms() {

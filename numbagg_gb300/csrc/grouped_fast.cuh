@@ -29,6 +29,8 @@
 // Private bins are updated in column order; shared and global bins with a 128-bit
 // compare-and-swap issued only when the element improves on the current pair.
 // first / last are a minimum / maximum of the column index.  All of these are exact.
+#pragma once
+
 #include "grouped_common.cuh"
 #include "fixed128.cuh"
 
@@ -1409,21 +1411,11 @@ int launch_ragged_group(const double* values, const L* labels, const long long* 
 }  // namespace nbg
 
 // ---------------------------------------------------------------------------------
-// exported entry points of the fast paths
+// exported entry points of the fast paths: the translation units grouped_fast_*.cu
+// each instantiate a share of them (they compile in parallel)
 // ---------------------------------------------------------------------------------
 namespace nbg {
 namespace grouped {
-size_t fast_bytes_query(int f, long long rows, long long m, long long K) {
-  if (!(is_moments(f) || is_select(f) || f == kFirst || f == kLast)) return 0;
-  return fast_bytes(f, rows, m, K);
-}
-}  // namespace grouped
-}  // namespace nbg
-
-using namespace nbg;
-using namespace nbg::grouped;
-
-namespace {
 template <int F, typename V, typename L, typename O>
 int group_fast_entry(const V* values, const L* labels, O* out, long long rows, long long m, long long K,
                      long long ddof, void* ws, size_t ws_bytes, cudaStream_t s) {
@@ -1434,55 +1426,16 @@ int group_fast_entry(const V* values, const L* labels, O* out, long long rows, l
   // m == 0 still runs: one chunk of no columns writes every output's empty value
   return launch_fast<F, V, L, O>(values, labels, out, rows, m, K, ddof, ws, ws_bytes, s);
 }
-}  // namespace
+}  // namespace grouped
+}  // namespace nbg
 
-extern "C" {
 #define NBG_GFAST_ONE(NAME, FC, V, VS, O, L, LS)                                               \
   int nbg_group_##NAME##_##VS##_##LS(const V* values, const L* labels, O* out, long long rows,  \
                                      long long m, long long num_labels, long long ddof, void* ws, \
                                      size_t ws_bytes, void* stream) {                          \
-    return group_fast_entry<FC, V, L, O>(values, labels, out, rows, m, num_labels, ddof, ws,    \
-                                         ws_bytes, static_cast<cudaStream_t>(stream));         \
+    return nbg::grouped::group_fast_entry<FC, V, L, O>(values, labels, out, rows, m, num_labels, \
+                                                       ddof, ws, ws_bytes,                      \
+                                                       static_cast<cudaStream_t>(stream));      \
   }
 #define NBG_GFAST_LABELS(NAME, FC, V, VS, O) \
   NBG_GFAST_ONE(NAME, FC, V, VS, O, int, i32) NBG_GFAST_ONE(NAME, FC, V, VS, O, long long, i64)
-#define NBG_GFAST_FLOAT(NAME, FC)                 \
-  NBG_GFAST_LABELS(NAME, FC, double, f64, double) \
-  NBG_GFAST_LABELS(NAME, FC, float, f32, float)
-#define NBG_GFAST_ALL(NAME, FC)                          \
-  NBG_GFAST_FLOAT(NAME, FC)                              \
-  NBG_GFAST_LABELS(NAME, FC, int, i32, int)              \
-  NBG_GFAST_LABELS(NAME, FC, long long, i64, long long)
-
-NBG_GFAST_FLOAT(nansum, kSum)
-NBG_GFAST_FLOAT(nancount, kCount)
-NBG_GFAST_FLOAT(nanmean, kMean)
-NBG_GFAST_FLOAT(nanvar, kVar)
-NBG_GFAST_FLOAT(nanstd, kStd)
-NBG_GFAST_FLOAT(nansum_of_squares, kSumSq)
-NBG_GFAST_ALL(nanargmax, kArgMax)
-NBG_GFAST_ALL(nanargmin, kArgMin)
-NBG_GFAST_ALL(nanmax, kMax)
-NBG_GFAST_ALL(nanmin, kMin)
-NBG_GFAST_ALL(nanfirst, kFirst)
-NBG_GFAST_ALL(nanlast, kLast)
-
-// Ragged series with their own labels: values, labels: `total` values in series
-// s = [offsets[s], offsets[s + 1]); out: nseries x num_labels (float64).
-size_t nbg_group_ragged_workspace_bytes(long long nseries, long long total, long long num_labels) {
-  return ragged_group_bytes(nseries < 0 ? 0 : nseries, total < 0 ? 0 : total, num_labels < 0 ? 0 : num_labels);
-}
-#define NBG_GRAGGED(NAME, FC, L, LS)                                                                 \
-  int nbg_group_##NAME##_ragged_f64_##LS(const double* values, const L* labels, const long long* offsets, \
-                                         long long nseries, long long total, long long num_labels,       \
-                                         double* out, void* ws, size_t ws_bytes, void* stream) {         \
-    return launch_ragged_group<FC, L>(values, labels, offsets, nseries, total, num_labels, out, ws,      \
-                                      ws_bytes, static_cast<cudaStream_t>(stream));                      \
-  }
-NBG_GRAGGED(nansum, kSum, int, i32)
-NBG_GRAGGED(nansum, kSum, long long, i64)
-NBG_GRAGGED(nanmean, kMean, int, i32)
-NBG_GRAGGED(nanmean, kMean, long long, i64)
-NBG_GRAGGED(nancount, kCount, int, i32)
-NBG_GRAGGED(nancount, kCount, long long, i64)
-}  // extern "C"

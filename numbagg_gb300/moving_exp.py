@@ -3,8 +3,14 @@
 Same names, keywords and checks as numbagg's ``ndmoveexp`` decorator
 (numbagg/decorators.py:374-414): ``alpha`` is a scalar, a 1-D array along the
 scanned axis, or an array shaped like the input; ``axis`` may be an int or a
-1-tuple, ``axis=()`` returns the input.  alpha and min_weight are rounded to the
-array dtype first, as the gufunc's float32 loop does.
+1-tuple, ``axis=()`` returns the input.
+
+The loop dtype follows numpy's resolution of the gufunc's two loops (float32,
+float64) over the array operands: numbagg turns a scalar alpha into
+``np.broadcast_to(alpha, n)``, a float64 array for a Python float, so float32 input
+with a scalar alpha runs (and returns) float64; the float32 loop runs only when the
+arrays and an alpha array all cast safely to float32.  alpha and min_weight are then
+rounded to the loop dtype.
 """
 
 from __future__ import annotations
@@ -16,6 +22,26 @@ from . import _host, _lib
 
 
 PRECISIONS = ("f64", "fp32c")
+
+
+def _operand_dtype(x) -> np.dtype:
+    if isinstance(x, torch.Tensor):
+        return np.dtype(str(x.dtype).replace("torch.", "")) if x.dtype != torch.bfloat16 else np.dtype(np.float32)
+    return np.asarray(x).dtype
+
+
+def loop_dtype(arrays, alpha, min_weight) -> torch.dtype:
+    """float32 when every array operand (the inputs, alpha broadcast as numbagg does it,
+    and min_weight when it is a numpy scalar) casts safely to float32, else float64:
+    the first of the gufunc's loops (float32, float64) that numpy's type resolution
+    accepts."""
+    dts = [_operand_dtype(x) for x in arrays]
+    dts.append(_operand_dtype(alpha))
+    if isinstance(min_weight, np.generic):
+        dts.append(min_weight.dtype)
+    if all(np.can_cast(d, np.float32, casting="safe") for d in dts):
+        return torch.float32
+    return torch.float64
 
 
 def _move_exp(name: str, arrs, alpha, min_weight, axis, precision="f64"):
@@ -44,10 +70,9 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis, precision="f64"):
         tensors.append(t)
         restore = restore or r
     a = tensors[0]
-    dtype = _host.float_compute_dtype(a.dtype)
+    dtype = loop_dtype(tensors, alpha, min_weight)
     if len(tensors) > 1:
         tensors = list(torch.broadcast_tensors(*tensors))
-        dtype = _host.float_compute_dtype(torch.promote_types(tensors[0].dtype, tensors[1].dtype))
     flats = []
     shape = None
     for t in tensors:

@@ -122,9 +122,20 @@ def move(name, a, b=None, *, window, min_count=None, axis=-1, nthreads=0, ext=Fa
 
 def move_exp(name, a, b=None, *, alpha, min_weight=0.0, axis=-1, nthreads=0, ext=False):
     """numbagg.move_exp_* restated (ndmoveexp.__call__, numbagg/decorators.py:374-414).
+
+    The loop dtype is numpy's choice between the gufunc's float32 and float64 loops
+    (numbagg/moving_exp.py:12-17): a scalar alpha becomes np.broadcast_to(alpha, n),
+    a float64 array for a Python float, so the float32 loop runs only when the arrays
+    and an alpha array all cast safely to float32.
     ext=True: long double accumulators, as for move()."""
     a = np.asarray(a)
-    dtype = np.dtype(a.dtype).newbyteorder("=")
+    operands = [a] + ([np.asarray(b)] if b is not None else [])
+    alpha_dt = alpha.dtype if isinstance(alpha, np.ndarray) else np.asarray(alpha).dtype
+    dts = [x.dtype for x in operands] + [alpha_dt]
+    if isinstance(min_weight, np.generic):
+        dts.append(min_weight.dtype)
+    f32 = all(np.can_cast(d, np.float32, casting="safe") for d in dts)
+    dtype = np.dtype(np.float32 if f32 else np.float64)
     dt = _F[dtype]
     fa, shape = _rows_last(a.astype(dtype, copy=False), axis)
     rows, n = fa.shape
@@ -135,7 +146,7 @@ def move_exp(name, a, b=None, *, alpha, min_weight=0.0, axis=-1, nthreads=0, ext
         al = np.ascontiguousarray(alpha.astype(dtype)).reshape(1, n)
         stride = 0
     else:
-        al, _ = _rows_last(alpha.astype(dtype), axis)
+        al, _ = _rows_last(np.broadcast_to(alpha, a.shape).astype(dtype), axis)
         stride = n
     out = np.empty_like(fa)
     mw = ctypes.c_double(min_weight) if dt == "f64" else ctypes.c_float(min_weight)

@@ -218,3 +218,42 @@ def exp_degenerate(name, a, b, alpha, min_weight, axis=-1):
     weight = np.where(np.isnan(weight), 0.0, weight)
     allow |= np.abs(weight - min_weight) <= 1e-12 * max(1.0, abs(min_weight))
     return allow
+
+
+def move_unresolved(name, a, b, window, k=64, axis=-1):
+    """Positions where float64 cannot resolve a window variance that the decision
+    rests on: move_std's sqrt of a negative residue (numbagg/moving.py:147-150) and
+    move_corr's `var_a * var_b > 0` (numbagg/moving.py:266-272) test a difference of
+    two numbers of size mean(x^2), so a true (pairwise) variance within k ulps of
+    mean(x^2) makes the NaN decision rounding noise in any float64 evaluation."""
+    if name not in ("move_std", "move_var", "move_corr", "move_cov"):
+        return None
+    v = _valid(a, b)
+    res = k * np.finfo(np.float64).eps
+    out = np.zeros(v.shape, bool)
+    for x in (a, b) if b is not None else (a,):
+        xm = np.where(v, np.asarray(x, dtype=np.float64), np.nan)
+        var = oracle.move("move_var", xm, window=window, min_count=2, axis=axis, ext=True)
+        msq = oracle.move("move_mean", xm * xm, window=window, min_count=1, axis=axis)
+        with np.errstate(invalid="ignore"):
+            out |= var <= res * msq
+    return out
+
+
+def exp_unresolved(name, a, b, alpha, k=256, axis=-1):
+    """The same for the exponentially weighted variance family: a weighted variance
+    within k ulps of the weighted mean of x^2 (numbagg/moving_exp.py:145-156,
+    :320-335)."""
+    if name not in ("move_exp_nanvar", "move_exp_nanstd", "move_exp_nancov", "move_exp_nancorr"):
+        return None
+    v = _valid(a, b)
+    res = k * np.finfo(np.float64).eps
+    al = alpha if not isinstance(alpha, np.ndarray) else alpha.astype(np.float64)
+    out = np.zeros(v.shape, bool)
+    for x in (a, b) if b is not None else (a,):
+        xm = np.where(v, np.asarray(x, dtype=np.float64), np.nan)
+        var = oracle.move_exp("move_exp_nanvar", xm, alpha=al, axis=axis, ext=True)
+        msq = oracle.move_exp("move_exp_nanmean", xm * xm, alpha=al, axis=axis)
+        with np.errstate(invalid="ignore"):
+            out |= var <= res * msq
+    return out

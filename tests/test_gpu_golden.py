@@ -67,7 +67,9 @@ def test_move_exp_golden(golden, fname):
         _, dt, atag, mw = key.split("|")
         x = golden[f"exp_in_{dt}"]
         b = golden[f"exp_in_b_{dt}"] if fname in ("move_exp_nancov", "move_exp_nancorr") else None
-        alpha = golden[f"exp_alpha_vec_{dt}"] if atag == "vec" else float(atag)
+        # the golden float32 runs used float32 alpha arrays, which select numbagg's
+        # float32 loop (a Python-float alpha would select the float64 one)
+        alpha = golden[f"exp_alpha_vec_{dt}"] if atag == "vec" else np.full(x.shape[-1], float(atag), dtype=x.dtype)
         mw = float(mw)
         got = func(x, b, alpha=alpha, min_weight=mw) if b is not None else func(x, alpha=alpha, min_weight=mw)
         want = golden[key]

@@ -27,8 +27,10 @@ from tests.parity import (
     assert_scaled_close,
     exp_degenerate,
     exp_scale,
+    exp_unresolved,
     move_degenerate,
     move_scale,
+    move_unresolved,
     parity_error,
 )
 
@@ -152,9 +154,10 @@ def test_precision_stress_plain_move(fname, window):
     ref = oracle.move(fname, a, y, window=window, min_count=mc)
     ext = oracle.move(fname, a, y, window=window, min_count=mc, ext=True)
     # where the reference and the extended result disagree on NaN (a variance whose
-    # rounding residue in the reference went negative, numbagg/moving.py:147-150), the
-    # reference's decision is noise; such positions are allowed and counted
-    allow = np.isnan(ref) != np.isnan(ext)
+    # rounding residue in the reference went negative, numbagg/moving.py:147-150), or
+    # where the window variance is below what float64 resolves on data of size 1e6,
+    # the NaN decision is rounding noise; such positions are allowed and counted
+    allow = (np.isnan(ref) != np.isnan(ext)) | move_unresolved(fname, a, y, window)
     deg = move_degenerate(fname, a, y, window)
     if deg is not None:
         allow |= deg
@@ -175,6 +178,9 @@ def test_precision_stress_plain_exp(fname, alpha):
     ref = oracle.move_exp(fname, a, y, alpha=alpha, min_weight=0)
     ext = oracle.move_exp(fname, a, y, alpha=alpha, min_weight=0, ext=True)
     allow = exp_degenerate(fname, a, y, alpha, 0.0) | (np.isnan(ref) != np.isnan(ext))
+    unresolved = exp_unresolved(fname, a, y, alpha)
+    if unresolved is not None:
+        allow |= unresolved
     r = assert_parity(got, ref, ext, exp_scale(fname, a, y, alpha), F64_TOL, allow, f"{fname} alpha={alpha}")
     assert r["allowed"] <= 0.01 * r["n"], r
     _report(f"{fname} alpha={alpha}", got, ref, ext)

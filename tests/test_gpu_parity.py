@@ -116,6 +116,16 @@ def test_move_exp_vs_oracle(fname, dtype, alpha, min_weight):
     x = _data((5, 30_000), 6, normal=False, dtype=dtype)
     y = _data((5, 30_000), 7, normal=False, dtype=dtype) if fname in ("move_exp_nancov", "move_exp_nancorr") else None
     func = getattr(nb, fname)
+    if dtype == np.float32:
+        # a float32 alpha array selects numbagg's float32 loop; a Python float alpha
+        # is broadcast to a float64 array and selects the float64 loop
+        wide = func(x, y, alpha=alpha, min_weight=min_weight) if y is not None else func(x, alpha=alpha, min_weight=min_weight)
+        assert wide.dtype == np.float64
+        x64 = x.astype(np.float64)
+        y64 = None if y is None else y.astype(np.float64)
+        ref64 = func(x64, y64, alpha=alpha, min_weight=min_weight) if y is not None else func(x64, alpha=alpha, min_weight=min_weight)
+        assert_bit_equal(wide, ref64, f"{fname} float32 input, float64 loop")
+        alpha = np.full(x.shape[-1], alpha, dtype=np.float32)
     got = func(x, y, alpha=alpha, min_weight=min_weight) if y is not None else func(x, alpha=alpha, min_weight=min_weight)
     want = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight)
     ext = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight, ext=True)
