@@ -250,6 +250,67 @@ def move_matrix(name, a, *, window, min_count=None, nthreads=0, ext=False):
     return out.reshape(a.shape[:-2] + (t_obs, n_vars, n_vars))
 
 
+def move_exp_matrix(name, a, *, alpha, min_weight=0.0, nthreads=0, ext=False):
+    """numbagg.move_exp_nancovmatrix / move_exp_nancorrmatrix restated
+    (ndmoveexpmatrix.__call__, numbagg/decorators.py:1061-1087): a (..., obs, vars),
+    alpha a scalar (broadcast along obs as np.broadcast_to does, hence float64 for a
+    Python float) or an array (..., obs).  The loop dtype is numpy's choice between the
+    float32 and float64 loops (numbagg/moving_matrix.py:204-212).  ext=True computes
+    in long double and returns float64."""
+    a = np.asarray(a)
+    if a.ndim < 2:
+        raise ValueError(f"{name} requires at least a 2D array with shape (..., obs, vars).")
+    if not isinstance(alpha, np.ndarray):
+        alpha = np.broadcast_to(alpha, a.shape[-2])
+    dts = [a.dtype, alpha.dtype] + ([min_weight.dtype] if isinstance(min_weight, np.generic) else [])
+    f32 = all(np.can_cast(d, np.float32, casting="safe") for d in dts)
+    dtype = np.dtype(np.float32 if f32 else np.float64)
+    dt = _F[dtype]
+    if ext:
+        dtype, dt = np.dtype(np.longdouble), "ld"
+    lead = np.broadcast_shapes(a.shape[:-2], alpha.shape[:-1])
+    t_obs, n_vars = a.shape[-2:]
+    fa = np.ascontiguousarray(np.broadcast_to(a, lead + (t_obs, n_vars)).astype(dtype)).reshape(-1, t_obs, n_vars)
+    if alpha.ndim == 1:
+        al = np.ascontiguousarray(alpha.astype(dtype)).reshape(1, t_obs)
+        stride = 0
+    else:
+        al = np.ascontiguousarray(np.broadcast_to(alpha, lead + (t_obs,)).astype(dtype)).reshape(-1, t_obs)
+        stride = t_obs
+    out = np.empty((fa.shape[0], t_obs, n_vars, n_vars), dtype=dtype)
+    mw = {"f64": ctypes.c_double, "f32": ctypes.c_float, "ld": ctypes.c_longdouble}[dt](min_weight)
+    getattr(lib(), f"orc_{name}_{dt}")(
+        _p(fa), _p(al), _i(stride), mw, _p(out), _i(fa.shape[0]), _i(t_obs), _i(n_vars), ctypes.c_int(nthreads)
+    )
+    if ext:
+        out = out.astype(np.float64)
+    return out.reshape(lead + (t_obs, n_vars, n_vars))
+
+
+def static_matrix(name, a, *, nthreads=0, ext=False):
+    """numbagg.nancovmatrix / nancorrmatrix restated (ndmatrix.__call__,
+    numbagg/decorators.py:700-717): a (..., vars, obs) -> (..., vars, vars), float32
+    or float64 (other dtypes take the first loop they cast to safely).  ext=True
+    computes in long double and returns float64."""
+    a = np.asarray(a)
+    if a.ndim < 2:
+        raise ValueError(
+            f"{name} requires at least a 2D array with shape (..., vars, obs). "
+            "For 1D arrays, use nanvar for variance calculations."
+        )
+    dtype = np.dtype(np.float32 if np.can_cast(a.dtype, np.float32, casting="safe") else np.float64)
+    dt = _F[dtype]
+    if ext:
+        dtype, dt = np.dtype(np.longdouble), "ld"
+    n_vars, n_obs = a.shape[-2:]
+    fa = np.ascontiguousarray(a.astype(dtype)).reshape(-1, n_vars, n_obs)
+    out = np.empty((fa.shape[0], n_vars, n_vars), dtype=dtype)
+    getattr(lib(), f"orc_{name}_{dt}")(_p(fa), _p(out), _i(fa.shape[0]), _i(n_vars), _i(n_obs), ctypes.c_int(nthreads))
+    if ext:
+        out = out.astype(np.float64)
+    return out.reshape(a.shape[:-2] + (n_vars, n_vars))
+
+
 __all__ = [
     "GROUP_FUNCS",
     "MOVE_EXP_FUNCS",
@@ -259,7 +320,9 @@ __all__ = [
     "lib",
     "move",
     "move_exp",
+    "move_exp_matrix",
     "move_matrix",
+    "static_matrix",
 ]
 
 

@@ -519,3 +519,223 @@ DEF_MOVE_MATRIX(double, f64)
 DEF_MOVE_MATRIX(float, f32)
 /* extended precision (long double arrays and accumulators) */
 DEF_MOVE_MATRIX(long double, ld)
+
+/* ------------------------------------------------------------------------------ */
+/* Exponentially weighted moving matrices: numbagg/moving_matrix.py:204-432.        */
+/* a (batch, T, V) C-contiguous; alpha: T values per batch entry, batch entry b at   */
+/* alpha_ + b * alpha_stride (stride 0: shared); out (batch, T, V, V).  The pair     */
+/* states are arrays of the input dtype (:245-263, :371-383).  `decay = 1.0 -        */
+/* alpha_t` is float64 in numba even for float32 input (a float64 literal minus a    */
+/* float32), so each state is multiplied in D and stored back in T; the additions    */
+/* of values and of alpha_t stay in T.  The finalisation follows the same typing:    */
+/* `1 - f32` and `f32 / bias` are float64, the means and biased moments are T.      */
+/* ------------------------------------------------------------------------------ */
+#define DEF_EXP_MATRIX(T, D, SFX, SQRT)                                                \
+  EXPORT int orc_move_exp_nancovmatrix_##SFX(const T* a_, const T* alpha_,            \
+      int64_t alpha_stride, T min_weight, T* out_, int64_t batch, int64_t n_obs,       \
+      int64_t n_vars, int nthreads) {                                                  \
+    int64_t VV = n_vars * n_vars;                                                      \
+    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
+    for (int64_t bi = 0; bi < batch; ++bi) {                                           \
+      const T* a = a_ + bi * n_obs * n_vars; const T* al = alpha_ + bi * alpha_stride; \
+      T* out = out_ + bi * n_obs * VV;                                                 \
+      T* si = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* pr = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* pw = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sw = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sw2 = (T*)calloc((size_t)VV + 1, sizeof(T));                                  \
+      for (int64_t t = 0; t < n_obs; ++t) {                                            \
+        T alpha_t = al[t];                                                             \
+        D decay = (D)1.0 - (D)alpha_t, decay2 = decay * decay;                         \
+        for (int64_t q = 0; q < VV; ++q) {                                             \
+          si[q] = (T)((D)si[q] * decay); sj[q] = (T)((D)sj[q] * decay);                \
+          pr[q] = (T)((D)pr[q] * decay); pw[q] = (T)((D)pw[q] * decay);                \
+          sw[q] = (T)((D)sw[q] * decay); sw2[q] = (T)((D)sw2[q] * decay2);             \
+        }                                                                              \
+        const T* nw = a + t * n_vars;                                                  \
+        for (int64_t i = 0; i < n_vars; ++i) {                                         \
+          T vi = nw[i]; if (isnan(vi)) continue;                                       \
+          for (int64_t j = 0; j < n_vars; ++j) {                                       \
+            T vj = nw[j]; if (isnan(vj)) continue;                                     \
+            int64_t q = i * n_vars + j;                                                \
+            si[q] = (T)(si[q] + vi); sj[q] = (T)(sj[q] + vj);                          \
+            pr[q] = (T)(pr[q] + (T)(vi * vj)); pw[q] = (T)(pw[q] + alpha_t);           \
+            sw[q] = (T)((D)sw[q] + (D)1.0); sw2[q] = (T)((D)sw2[q] + (D)1.0);          \
+          }                                                                            \
+        }                                                                              \
+        T* ot = out + t * VV;                                                          \
+        for (int64_t q = 0; q < VV; ++q) {                                             \
+          T n = sw[q];                                                                 \
+          D bias = n > 0 ? (D)1 - (D)(T)(sw2[q] / (T)(n * n)) : (D)0.0;                \
+          if (pw[q] >= min_weight && bias > 0) {                                       \
+            T mi = (T)(si[q] / n), mj = (T)(sj[q] / n);                                \
+            T cb = (T)((T)(pr[q] / n) - (T)(mi * mj));                                 \
+            ot[q] = (T)((D)cb / bias);                                                 \
+          } else {                                                                     \
+            ot[q] = (T)NAN;                                                            \
+          }                                                                            \
+        }                                                                              \
+      }                                                                                \
+      free(si); free(sj); free(pr); free(pw); free(sw); free(sw2);                     \
+    }                                                                                  \
+    return 0;                                                                          \
+  }                                                                                    \
+  EXPORT int orc_move_exp_nancorrmatrix_##SFX(const T* a_, const T* alpha_,           \
+      int64_t alpha_stride, T min_weight, T* out_, int64_t batch, int64_t n_obs,       \
+      int64_t n_vars, int nthreads) {                                                  \
+    int64_t VV = n_vars * n_vars;                                                      \
+    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
+    for (int64_t bi = 0; bi < batch; ++bi) {                                           \
+      const T* a = a_ + bi * n_obs * n_vars; const T* al = alpha_ + bi * alpha_stride; \
+      T* out = out_ + bi * n_obs * VV;                                                 \
+      T* si = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* qi = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* qj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* pr = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* pw = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sw = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sw2 = (T*)calloc((size_t)VV + 1, sizeof(T));                                  \
+      for (int64_t t = 0; t < n_obs; ++t) {                                            \
+        T alpha_t = al[t];                                                             \
+        D decay = (D)1.0 - (D)alpha_t, decay2 = decay * decay;                         \
+        for (int64_t q = 0; q < VV; ++q) {                                             \
+          si[q] = (T)((D)si[q] * decay); sj[q] = (T)((D)sj[q] * decay);                \
+          qi[q] = (T)((D)qi[q] * decay); qj[q] = (T)((D)qj[q] * decay);                \
+          pr[q] = (T)((D)pr[q] * decay); pw[q] = (T)((D)pw[q] * decay);                \
+          sw[q] = (T)((D)sw[q] * decay); sw2[q] = (T)((D)sw2[q] * decay2);             \
+        }                                                                              \
+        const T* nw = a + t * n_vars;                                                  \
+        for (int64_t i = 0; i < n_vars; ++i) {                                         \
+          T vi = nw[i]; if (isnan(vi)) continue;                                       \
+          for (int64_t j = 0; j < n_vars; ++j) {                                       \
+            T vj = nw[j]; if (isnan(vj)) continue;                                     \
+            int64_t q = i * n_vars + j;                                                \
+            si[q] = (T)(si[q] + vi); sj[q] = (T)(sj[q] + vj);                          \
+            qi[q] = (T)(qi[q] + (T)(vi * vi)); qj[q] = (T)(qj[q] + (T)(vj * vj));      \
+            pr[q] = (T)(pr[q] + (T)(vi * vj)); pw[q] = (T)(pw[q] + alpha_t);           \
+            sw[q] = (T)((D)sw[q] + (D)1.0); sw2[q] = (T)((D)sw2[q] + (D)1.0);          \
+          }                                                                            \
+        }                                                                              \
+        T* ot = out + t * VV;                                                          \
+        for (int64_t q = 0; q < VV; ++q) {                                             \
+          T n = sw[q];                                                                 \
+          D bias = n > 0 ? (D)1 - (D)(T)(sw2[q] / (T)(n * n)) : (D)0.0;                \
+          if (pw[q] >= min_weight && bias > 0) {                                       \
+            T mi = (T)(si[q] / n), mj = (T)(sj[q] / n);                                \
+            T vib = (T)((T)(qi[q] / n) - (T)(mi * mi));                                \
+            T vjb = (T)((T)(qj[q] / n) - (T)(mj * mj));                                \
+            T cb = (T)((T)(pr[q] / n) - (T)(mi * mj));                                 \
+            D vi = (D)vib / bias, vj = (D)vjb / bias, cv = (D)cb / bias;               \
+            ot[q] = (T)((vi > 0 && vj > 0) ? cv / SQRT(vi * vj) : (D)NAN);             \
+          } else {                                                                     \
+            ot[q] = (T)NAN;                                                            \
+          }                                                                            \
+        }                                                                              \
+      }                                                                                \
+      free(si); free(sj); free(qi); free(qj); free(pr); free(pw); free(sw); free(sw2); \
+    }                                                                                  \
+    return 0;                                                                          \
+  }
+
+DEF_EXP_MATRIX(double, double, f64, sqrt)
+DEF_EXP_MATRIX(float, double, f32, sqrt)
+DEF_EXP_MATRIX(long double, long double, ld, sqrtl)
+
+/* ------------------------------------------------------------------------------ */
+/* Static pairwise-complete matrices: numbagg/funcs.py:338-532.  a (batch, V, n_obs) */
+/* C-contiguous, out (batch, V, V).  Sums in the input dtype over the upper          */
+/* triangle, observation by observation (:414-430, :508-520), int64 counts; the     */
+/* finalisation divides a T sum by an int64 count, which numba types as float64     */
+/* (:433-456, :523-532).                                                             */
+/* ------------------------------------------------------------------------------ */
+#define DEF_STATIC_MATRIX(T, D, SFX, SQRT)                                             \
+  EXPORT int orc_nancovmatrix_##SFX(const T* a_, T* out_, int64_t batch,              \
+      int64_t n_vars, int64_t n_obs, int nthreads) {                                   \
+    int64_t VV = n_vars * n_vars;                                                      \
+    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
+    for (int64_t bi = 0; bi < batch; ++bi) {                                           \
+      const T* a = a_ + bi * n_vars * n_obs; T* out = out_ + bi * VV;                  \
+      T* si = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sij = (T*)calloc((size_t)VV + 1, sizeof(T));                                  \
+      int64_t* cnt = (int64_t*)calloc((size_t)VV + 1, sizeof(int64_t));                \
+      for (int64_t k = 0; k < n_obs; ++k) {                                            \
+        for (int64_t i = 0; i < n_vars; ++i) {                                         \
+          T vi = a[i * n_obs + k]; if (isnan(vi)) continue;                            \
+          for (int64_t j = i; j < n_vars; ++j) {                                       \
+            T vj = a[j * n_obs + k]; if (isnan(vj)) continue;                          \
+            int64_t q = i * n_vars + j;                                                \
+            si[q] = (T)(si[q] + vi); sj[q] = (T)(sj[q] + vj);                          \
+            sij[q] = (T)(sij[q] + (T)(vi * vj)); cnt[q] += 1;                          \
+          }                                                                            \
+        }                                                                              \
+      }                                                                                \
+      for (int64_t i = 0; i < n_vars; ++i) {                                           \
+        for (int64_t j = i; j < n_vars; ++j) {                                         \
+          int64_t q = i * n_vars + j, c = cnt[q];                                      \
+          T r;                                                                         \
+          if (c > 1) {                                                                 \
+            D dc = (D)c;                                                               \
+            D mi = (D)si[q] / dc, mj = (D)sj[q] / dc;                                  \
+            D cov = (D)sij[q] / dc - mi * mj;                                          \
+            r = (T)(cov * dc / (D)(c - 1));                                            \
+          } else {                                                                     \
+            r = (T)NAN;                                                                \
+          }                                                                            \
+          out[q] = r; out[j * n_vars + i] = r;                                         \
+        }                                                                              \
+      }                                                                                \
+      free(si); free(sj); free(sij); free(cnt);                                        \
+    }                                                                                  \
+    return 0;                                                                          \
+  }                                                                                    \
+  EXPORT int orc_nancorrmatrix_##SFX(const T* a_, T* out_, int64_t batch,             \
+      int64_t n_vars, int64_t n_obs, int nthreads) {                                   \
+    int64_t VV = n_vars * n_vars;                                                      \
+    _Pragma("omp parallel for schedule(static) num_threads(orc_threads(nthreads))")    \
+    for (int64_t bi = 0; bi < batch; ++bi) {                                           \
+      const T* a = a_ + bi * n_vars * n_obs; T* out = out_ + bi * VV;                  \
+      T* si = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* qi = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* qj = (T*)calloc((size_t)VV + 1, sizeof(T));                                   \
+      T* sij = (T*)calloc((size_t)VV + 1, sizeof(T));                                  \
+      int64_t* cnt = (int64_t*)calloc((size_t)VV + 1, sizeof(int64_t));                \
+      for (int64_t k = 0; k < n_obs; ++k) {                                            \
+        for (int64_t i = 0; i < n_vars; ++i) {                                         \
+          T vi = a[i * n_obs + k]; if (isnan(vi)) continue;                            \
+          for (int64_t j = i; j < n_vars; ++j) {                                       \
+            T vj = a[j * n_obs + k]; if (isnan(vj)) continue;                          \
+            int64_t q = i * n_vars + j;                                                \
+            si[q] = (T)(si[q] + vi); sj[q] = (T)(sj[q] + vj);                          \
+            qi[q] = (T)(qi[q] + (T)(vi * vi)); qj[q] = (T)(qj[q] + (T)(vj * vj));      \
+            sij[q] = (T)(sij[q] + (T)(vi * vj)); cnt[q] += 1;                          \
+          }                                                                            \
+        }                                                                              \
+      }                                                                                \
+      for (int64_t i = 0; i < n_vars; ++i) {                                           \
+        for (int64_t j = i; j < n_vars; ++j) {                                         \
+          int64_t q = i * n_vars + j, c = cnt[q];                                      \
+          T r = (T)NAN;                                                                \
+          if (c > 1) {                                                                 \
+            D dc = (D)c;                                                               \
+            D mi = (D)si[q] / dc, mj = (D)sj[q] / dc;                                  \
+            D vi = (D)qi[q] / dc - mi * mi, vj = (D)qj[q] / dc - mj * mj;              \
+            D viu = vi * dc / (D)(c - 1), vju = vj * dc / (D)(c - 1);                  \
+            D cov = (D)sij[q] / dc - mi * mj;                                          \
+            D covu = cov * dc / (D)(c - 1);                                            \
+            if (viu > 0 && vju > 0) r = (T)(covu / SQRT(viu * vju));                   \
+          }                                                                            \
+          out[q] = r; out[j * n_vars + i] = r;                                         \
+        }                                                                              \
+      }                                                                                \
+      free(si); free(sj); free(qi); free(qj); free(sij); free(cnt);                    \
+    }                                                                                  \
+    return 0;                                                                          \
+  }
+
+DEF_STATIC_MATRIX(double, double, f64, sqrt)
+DEF_STATIC_MATRIX(float, double, f32, sqrt)
+DEF_STATIC_MATRIX(long double, long double, ld, sqrtl)

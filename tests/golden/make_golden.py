@@ -324,6 +324,40 @@ def generate(src: str) -> dict[str, np.ndarray]:
                     with np.errstate(all="ignore"):
                         body(a, w, mcv, out)
                     vec[f"{fname}|{dt}|{w}|{mc}"] = out
+
+    # ---- exponentially weighted matrices (numbagg/moving_matrix.py:204-432) -------
+    emat = _fixture_array((30, 4), seed=12)
+    emat[7, :] = np.nan  # a step with no valid variable
+    ealpha = np.linspace(0.05, 0.8, 30)
+    for dt in ("f64", "f32"):
+        dtype = np.float64 if dt == "f64" else np.float32
+        a = emat.astype(dtype)
+        vec[f"ematrix_in_{dt}"] = a
+        vec[f"ematrix_alpha_vec_{dt}"] = ealpha.astype(dtype)
+        for fname in ("move_exp_nancovmatrix", "move_exp_nancorrmatrix"):
+            body = _as_compiled(getattr(nb, fname).func)
+            for atag in ("0.5", "0.1", "vec"):
+                al = ealpha.astype(dtype) if atag == "vec" else np.full(30, float(atag), dtype=dtype)
+                for mw in (0.0, 0.5):
+                    out = np.empty((30, 4, 4), dtype=dtype)
+                    with np.errstate(all="ignore"):
+                        body(a, al, dtype(mw), out)
+                    vec[f"{fname}|{dt}|{atag}|{mw}"] = out
+
+    # ---- static pairwise-complete matrices (numbagg/funcs.py:338-532) -------------
+    smat = _fixture_array((5, 40), seed=13)
+    smat[4, :] = np.nan  # a variable with no observation
+    smat[3, 2:] = np.nan  # a variable with two observations
+    for dt in ("f64", "f32"):
+        dtype = np.float64 if dt == "f64" else np.float32
+        a = smat.astype(dtype)
+        vec[f"smatrix_in_{dt}"] = a
+        for fname in ("nancovmatrix", "nancorrmatrix"):
+            body = _as_compiled(getattr(nb, fname).func)
+            out = np.empty((5, 5), dtype=dtype)
+            with np.errstate(all="ignore"):
+                body(a, out)
+            vec[f"{fname}|{dt}"] = out
     return vec
 
 
