@@ -283,6 +283,42 @@ NBG_DECL_MATRIX(move_covmatrix, float, f32)
 NBG_DECL_MATRIX(move_corrmatrix, double, f64)
 NBG_DECL_MATRIX(move_corrmatrix, float, f32)
 
+/* ---- exponentially weighted covariance / correlation matrices -------------------------
+ * Replaces the gufuncs built by ndmoveexpmatrix (numbagg/decorators.py:1031-1100) from
+ *   move_exp_nancorrmatrix numbagg/moving_matrix.py:204-320
+ *   move_exp_nancovmatrix  numbagg/moving_matrix.py:323-432
+ * signature "(m,n),(m),()->(m,n,n)": a batch x n_obs x n_vars, alpha n_obs values per batch
+ * entry at alpha + b * alpha_stride (alpha_stride 0: one alpha row shared by the batch),
+ * out batch x n_obs x n_vars x n_vars.  min_weight is the array-dtype value widened to
+ * double.  ws: nbg_move_exp_matrix_workspace_bytes(corr, f64, batch, n_obs, n_vars) bytes of
+ * scratch (per-segment aggregates), no initialisation. */
+NBG_API size_t nbg_move_exp_matrix_workspace_bytes(int corr, int f64, long long batch, long long n_obs,
+                                                   long long n_vars);
+#define NBG_DECL_EXP_MATRIX(NAME, T, SFX)                                                                  \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, const T* alpha, long long alpha_stride, double min_weight, T* out, \
+                                 long long batch, long long n_obs, long long n_vars, void* ws, size_t ws_bytes, \
+                                 void* stream);
+NBG_DECL_EXP_MATRIX(move_exp_nancovmatrix, double, f64)
+NBG_DECL_EXP_MATRIX(move_exp_nancovmatrix, float, f32)
+NBG_DECL_EXP_MATRIX(move_exp_nancorrmatrix, double, f64)
+NBG_DECL_EXP_MATRIX(move_exp_nancorrmatrix, float, f32)
+
+/* ---- static pairwise-complete covariance / correlation matrices -----------------------
+ * Replaces the gufuncs built by ndmatrix (numbagg/decorators.py:677-744) from
+ *   nancorrmatrix numbagg/funcs.py:338-451     nancovmatrix numbagg/funcs.py:454-532
+ * signature "(n,m)->(n,n)": a batch x n_vars x n_obs, out batch x n_vars x n_vars (both
+ * triangles written).  ws: nbg_pair_matrix_workspace_bytes(corr, f64, batch, n_vars, n_obs)
+ * bytes of scratch (per-slice partial sums, folded in slice order), no initialisation. */
+NBG_API size_t nbg_pair_matrix_workspace_bytes(int corr, int f64, long long batch, long long n_vars,
+                                               long long n_obs);
+#define NBG_DECL_PAIR_MATRIX(NAME, T, SFX)                                                                  \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long batch, long long n_vars, long long n_obs, void* ws, \
+                                 size_t ws_bytes, void* stream);
+NBG_DECL_PAIR_MATRIX(nancovmatrix, double, f64)
+NBG_DECL_PAIR_MATRIX(nancovmatrix, float, f32)
+NBG_DECL_PAIR_MATRIX(nancorrmatrix, double, f64)
+NBG_DECL_PAIR_MATRIX(nancorrmatrix, float, f32)
+
 /* ---- static aggregations over the last axis ----------------------------------------
  * Replace numbagg/funcs.py:23-159 (ndaggregate: allnan, anynan, nancount, nansum,
  * nanmean, nanvar, nanstd) and :162-242 (ndreduce: nanargmax, nanargmin, nanmax,

@@ -21,7 +21,7 @@ from .aggregate import (
     nansum,
     nanvar,
 )
-from .funcs import bfill, ffill
+from .funcs import bfill, ffill, nancorrmatrix, nancovmatrix
 from .grouped import (
     group_nanall,
     group_nanany,
@@ -49,13 +49,13 @@ from .moving_exp import (
     move_exp_nansum,
     move_exp_nanvar,
 )
-from .moving_matrix import move_corrmatrix, move_covmatrix
+from .moving_matrix import move_corrmatrix, move_covmatrix, move_exp_nancorrmatrix, move_exp_nancovmatrix
 from . import ragged  # noqa: E402  (ragged batches: an extension)
 
 __version__ = "1.0.0"
 
 # category lists, as numbagg/__init__.py:64-127 (restricted to this package's path;
-# nanmedian / nanquantile and the static / EWM matrices are not built)
+# nanmedian / nanquantile are not built)
 AGGREGATION_FUNCS = [
     allnan,
     anynan,
@@ -96,13 +96,17 @@ MOVE_EXP_FUNCS = [
     move_exp_nansum,
     move_exp_nanvar,
 ]
+MOVE_EXP_MATRIX_FUNCS = [move_exp_nancorrmatrix, move_exp_nancovmatrix]
 MOVE_FUNCS = [move_corr, move_cov, move_mean, move_corrmatrix, move_covmatrix, move_std, move_sum, move_var]
+MATRIX_FUNCS = [nancorrmatrix, nancovmatrix]
 OTHER_FUNCS = [bfill, ffill]
 
 __all__ = [
     "AGGREGATION_FUNCS",
     "GROUPED_FUNCS",
+    "MATRIX_FUNCS",
     "MOVE_EXP_FUNCS",
+    "MOVE_EXP_MATRIX_FUNCS",
     "MOVE_FUNCS",
     "OTHER_FUNCS",
     "allnan",
@@ -130,8 +134,10 @@ __all__ = [
     "move_cov",
     "move_covmatrix",
     "move_exp_nancorr",
+    "move_exp_nancorrmatrix",
     "move_exp_nancount",
     "move_exp_nancov",
+    "move_exp_nancovmatrix",
     "move_exp_nanmean",
     "move_exp_nanstd",
     "move_exp_nansum",
@@ -142,7 +148,9 @@ __all__ = [
     "move_var",
     "nanargmax",
     "nanargmin",
+    "nancorrmatrix",
     "nancount",
+    "nancovmatrix",
     "nanmax",
     "nanmean",
     "nanmin",

@@ -66,6 +66,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     sig("nbg_ffill_f64_noalloc", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp)
     sig("nbg_ffill_noalloc_error", c_i, ctypes.POINTER(c_i), ctypes.POINTER(ctypes.c_uint), c_vp)
     sig("nbg_group_workspace_bytes", c_sz, c_i, c_ll, c_ll, c_ll)
+    sig("nbg_move_exp_matrix_workspace_bytes", c_sz, c_i, c_i, c_ll, c_ll, c_ll)
+    sig("nbg_pair_matrix_workspace_bytes", c_sz, c_i, c_i, c_ll, c_ll, c_ll)
     for dt in ("f64", "f32"):
         for f in ("move_sum", "move_mean", "move_var", "move_std"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
@@ -77,6 +79,10 @@ def _declare(lib: ctypes.CDLL) -> None:
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
         for f in ("move_covmatrix", "move_corrmatrix"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
+        for f in ("move_exp_nancovmatrix", "move_exp_nancorrmatrix"):
+            sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_d, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+        for f in ("nancovmatrix", "nancorrmatrix"):
+            sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
     # FP32-compensated forms of the float64 scans
     for f in ("move_sum", "move_mean", "move_var", "move_std"):
         sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)

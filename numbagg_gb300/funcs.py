@@ -1,4 +1,5 @@
-"""ffill / bfill (numbagg/funcs.py:294-326), on CUDA.
+"""ffill / bfill (numbagg/funcs.py:294-326) and the static pairwise-complete
+matrices nancorrmatrix / nancovmatrix (numbagg/funcs.py:338-532), on CUDA.
 
 Same keywords and checks as numbagg's ``ndfill`` decorator
 (numbagg/decorators.py:465-487): ``limit=None`` means the length of the axis, a
@@ -11,6 +12,8 @@ from __future__ import annotations
 
 import numpy as np
 import torch
+
+import math
 
 from . import _host, _lib
 
@@ -81,4 +84,55 @@ def bfill(arr, *, limit=None, axis=-1):
     return _fill("bfill", arr, limit, axis)
 
 
-__all__ = ["bfill", "ffill"]
+def _static_matrix(name: str, a):
+    """ndmatrix.__call__ (numbagg/decorators.py:700-717): (..., vars, obs) ->
+    (..., vars, vars); float32 input keeps the float32 loop, everything else that
+    casts safely runs the float64 one."""
+    shape = _host.shape_of(a)
+    if len(shape) < 2:
+        raise ValueError(
+            f"{name} requires at least a 2D array with shape (..., vars, obs). "
+            "For 1D arrays, use nanvar for variance calculations."
+        )
+    from .moving_exp import loop_dtype
+
+    t, restore = _host.to_device(a)
+    dtype = loop_dtype([t], np.float32(0), 0.0)
+    n_vars, n_obs = t.shape[-2:]
+    lead = tuple(t.shape[:-2])
+    batch = math.prod(lead)
+    flat = t.to(dtype).contiguous().reshape(batch, n_vars, n_obs)
+    out = torch.empty((batch, n_vars, n_vars), dtype=dtype, device=t.device)
+    if out.numel():
+        L = _lib.lib()
+        corr = 1 if name == "nancorrmatrix" else 0
+        f64 = 1 if dtype == torch.float64 else 0
+        fn = getattr(L, f"nbg_{name}_{_host.FLOAT_SFX[dtype]}")
+        for b0 in range(0, batch, 65535):
+            b1 = min(batch, b0 + 65535)
+            ws = _lib.workspaces.scratch(L.nbg_pair_matrix_workspace_bytes(corr, f64, b1 - b0, n_vars, n_obs), t.device)
+            _lib.check(
+                fn(flat[b0:b1].data_ptr(), out[b0:b1].data_ptr(), b1 - b0, n_vars, n_obs, ws.data_ptr(), ws.numel(),
+                   _host.stream(t.device)),
+                name,
+            )
+    return restore(out.reshape(lead + (n_vars, n_vars)))
+
+
+def nancorrmatrix(a, **kwargs):
+    """Pairwise-complete correlation matrix of the variables (axis -2) over the
+    observations (axis -1), NaN as missing (numbagg/funcs.py:338-451)."""
+    if kwargs:
+        raise TypeError(f"unexpected keyword arguments: {sorted(kwargs)}")
+    return _static_matrix("nancorrmatrix", a)
+
+
+def nancovmatrix(a, **kwargs):
+    """Pairwise-complete covariance matrix of the variables (axis -2) over the
+    observations (axis -1), NaN as missing (numbagg/funcs.py:454-532)."""
+    if kwargs:
+        raise TypeError(f"unexpected keyword arguments: {sorted(kwargs)}")
+    return _static_matrix("nancovmatrix", a)
+
+
+__all__ = ["bfill", "ffill", "nancorrmatrix", "nancovmatrix"]

@@ -81,7 +81,10 @@ def test_move_exp_fp32c(fname, kind):
 def test_fp32c_float32_input_runs_the_plain_form():
     x = np.random.default_rng(3).standard_normal((2, 500)).astype(np.float32)
     np.testing.assert_array_equal(nb.move_mean(x, window=7, precision="fp32c"), nb.move_mean(x, window=7))
-    np.testing.assert_array_equal(nb.move_exp_nanmean(x, alpha=0.1, precision="fp32c"), nb.move_exp_nanmean(x, alpha=0.1))
+    # a float32 alpha array keeps numbagg's float32 loop (a Python float alpha selects
+    # the float64 one, where the compensated form applies)
+    al = np.full(x.shape[-1], 0.1, dtype=np.float32)
+    np.testing.assert_array_equal(nb.move_exp_nanmean(x, alpha=al, precision="fp32c"), nb.move_exp_nanmean(x, alpha=al))
 
 
 def test_fp32c_deterministic_and_causal():
