@@ -857,6 +857,70 @@ __global__ void __launch_bounds__(FT, 2) big_mom_kernel(const V* __restrict__ va
 }
 
 
+// Variance / standard deviation with many labels.  Both moments of RB rows of one label
+// sit in 2 RB consecutive words, acc[((rb K + k) RB + r) 2 + m] (m = 0: sum, 1: sum of
+// squares), and one reduction instruction of a warp covers 32 / (2 RB) columns with
+// 2 RB lanes each: lane (r = (lane / 2) % RB, m = lane % 2) adds x or x * x of row r.
+// A label's whole span -- 32 bytes for RB = 2 -- is reduced by one instruction instead
+// of one per moment, which halves the L2 sector operations that bound this kernel.
+template <int F, typename V, typename L, int RB>
+__global__ void __launch_bounds__(FT, 2) big_var_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+                                                     long long rows, long long m, long long K, long long chunk_len,
+                                                     long long chunks, double* __restrict__ acc,
+                                                     unsigned* __restrict__ nanc) {
+  typedef typename BitsOf<V>::type B;
+  constexpr int U = kBigT / RB;
+  constexpr int LPC = 2 * RB;   // lanes per column
+  constexpr int CPI = 32 / LPC;  // columns per instruction
+  __shared__ BigStage<B, RB> st;
+  const long long rb = blockIdx.x / chunks, chunk = blockIdx.x - rb * chunks;
+  const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = (lane >> 1) % RB, mom = lane & 1, q = lane / LPC;
+  const long long row0 = rb * RB;
+  const bool live = row0 + r < rows;
+  const long long off = rb * K * RB + r;  // (label l, row r): off + l * RB
+  const unsigned long long stream = l2_evict_first();
+  const unsigned long long keep = l2_evict_last();
+  for (long long cbase = c0 + static_cast<long long>(warp) * 32 * U; cbase < c1;
+       cbase += static_cast<long long>(FT / 32) * 32 * U) {
+    B x[U][RB];
+    int lab[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long col = cbase + u * 32 + lane;
+      const bool in = col < c1;
+      lab[u] = in ? static_cast<int>(ld_hint(labels + col, stream)) : -1;
+#pragma unroll
+      for (int rr = 0; rr < RB; ++rr)
+        x[u][rr] = (in && row0 + rr < rows) ? ld_hint(as_bits(values) + (row0 + rr) * m + col, stream) : B(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int rr = 0; rr < RB; ++rr) st.s[warp][u][rr][lane] = x[u][rr];
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int i = 0; i < LPC; ++i) {
+        const int c = i * CPI + q;
+        const B e = st.s[warp][u][r][c];
+        const long long l = __shfl_sync(0xffffffffu, lab[u], c);
+        if (!live || l < 0 || l >= K) continue;
+        const long long a = off + l * RB;
+        if (nan_bits(e)) {
+          if (mom == 0) red_add_hint(&nanc[a], 1u, keep);
+          continue;
+        }
+        const double v = bits_to_f64(e);
+        red_add_hint(&acc[2 * a + mom], mom ? v * v : v, keep);
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // Selection with many labels, in two passes of fire-and-forget L2 reductions (no
 // compare-and-swap round trips): pass 0 reduces every bin's order key with max
 // (first / last: the column with min / max, which finishes the job); pass 1 reads the
@@ -1053,7 +1117,8 @@ __global__ void ragged_fold_kernel(const MomPart* __restrict__ parts, double* __
   }
 }
 
-// accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]
+// accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]; for the
+// variance and standard deviation both moments are interleaved, acc1[2 t + m]
 template <int F, typename O, int RB>
 __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
                                       const unsigned* __restrict__ nanc, const unsigned* __restrict__ hist,
@@ -1065,8 +1130,15 @@ __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const dou
     const long long rb = t / (K * RB), rem = t - rb * K * RB;
     const long long k = rem / RB, row = rb * RB + (rem - k * RB);
     if (row >= rows) continue;
-    const double s1 = Need<F>::s1 ? acc1[t] : 0.0;
-    const double s2 = Need<F>::s2 ? acc2[t] : 0.0;
+    double s1 = 0.0, s2 = 0.0;
+    if (Need<F>::varlike) {
+      const double2 p = reinterpret_cast<const double2*>(acc1)[t];
+      s1 = p.x;
+      s2 = p.y;
+    } else {
+      s1 = Need<F>::s1 ? acc1[t] : 0.0;
+      s2 = Need<F>::s2 ? acc2[t] : 0.0;
+    }
     const long long cnt = Need<F>::cnt ? static_cast<long long>(hist[k]) - nanc[t] : 1;
     // infinities are already in the float64 sums (inf + x, inf - inf = NaN)
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
@@ -1076,8 +1148,17 @@ __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const dou
     else if (F == kSumSq) res = static_cast<O>(s2);
     else if (F == kMean) res = static_cast<O>(cnt == 0 ? nan : div_by_count(s1, cnt, rcp));
     else {
+      // (s2 - s1^2 / c) / (c - ddof), numbagg/grouped.py:170-176, with the divisions as
+      // products by the tabled reciprocals (within an ulp of each quotient; the
+      // subtraction's cancellation is the reference's own)
       const long long denom = cnt - ddof;
-      double v = denom <= 0 ? nan : div_by_count(s2 - div_by_count(s1 * s1, cnt, rcp), denom, rcp);
+      double v = nan;
+      if (denom > 0) {
+        const bool tab = cnt <= kRcpN && denom <= kRcpN;
+        const double rc = tab ? __ldg(rcp + cnt) : 1.0 / static_cast<double>(cnt);
+        const double rd = tab ? __ldg(rcp + denom) : 1.0 / static_cast<double>(denom);
+        v = (s2 - s1 * (s1 * rc)) * rd;
+      }
       if (F == kStd) v = sqrt(v);
       res = static_cast<O>(v);
     }
@@ -1250,14 +1331,15 @@ template <int F, typename V, typename L, typename O, int RB>
 int launch_big_mom(const V* values, const L* labels, O* out, long long rows, long long m, long long K, long long ddof,
                    const FastPlan& p, unsigned char*& cur, cudaStream_t s) {
   const long long slots = p.blocks * RB * K;
-  double* acc1 = carve<double>(cur, slots);
-  double* acc2 = carve<double>(cur, Need<F>::s2 ? slots : 1);
+  // variance / standard deviation: both moments interleaved in acc1 (big_var_kernel)
+  double* acc1 = carve<double>(cur, Need<F>::varlike ? 2 * slots : slots);
+  double* acc2 = carve<double>(cur, (Need<F>::s2 && !Need<F>::varlike) ? slots : 1);
   unsigned* nanc = carve<unsigned>(cur, slots);
   unsigned* hist = carve<unsigned>(cur, K);
   double* rcp = carve<double>(cur, kRcpN + 1);
   int launches = 0;
-  if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * 8, s);
-  if (Need<F>::s2) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
+  if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * (Need<F>::varlike ? 16 : 8), s);
+  if (Need<F>::s2 && !Need<F>::varlike) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
   if (Need<F>::cnt) {
     cudaMemsetAsync(nanc, 0, static_cast<size_t>(slots) * 4, s);
     cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
@@ -1271,8 +1353,12 @@ int launch_big_mom(const V* values, const L* labels, O* out, long long rows, lon
     }
     ++launches;
   }
-  big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len,
-                                                                                   p.chunks, acc1, acc2, nanc);
+  if (Need<F>::varlike)
+    big_var_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K,
+                                                                                     p.chunk_len, p.chunks, acc1, nanc);
+  else
+    big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K,
+                                                                                     p.chunk_len, p.chunks, acc1, acc2, nanc);
   big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
   return launches + 2;
 }

@@ -19,6 +19,32 @@ def _cov_scale(ext):
     return np.sqrt(d[..., :, None] * d[..., None, :])
 
 
+def _cond(msq, var):
+    with np.errstate(invalid="ignore", divide="ignore"):
+        c = np.where(var > 0, msq / np.where(var > 0, var, 1.0), np.inf)
+    return np.where(np.isnan(c), np.inf, c)
+
+
+def _exp_corr_scale(a, alpha):
+    """max(1, cond_i, cond_j) with cond = EWM mean of x^2 / EWM variance of each variable:
+    how much the variance cancellation amplifies rounding in a correlation."""
+    x = np.moveaxis(np.asarray(a, dtype=np.float64), -1, -2)  # (..., V, T)
+    al = np.moveaxis(np.broadcast_to(alpha, a.shape[:-1])[..., None, :], -2, -2) if isinstance(alpha, np.ndarray) else alpha
+    if isinstance(al, np.ndarray):
+        al = np.broadcast_to(al, x.shape)
+    msq = oracle.move_exp("move_exp_nanmean", x * x, alpha=al)
+    var = oracle.move_exp("move_exp_nanvar", x, alpha=al)
+    c = np.moveaxis(_cond(msq, var), -1, -2)  # (..., T, V)
+    return np.fmax(1.0, np.fmax(c[..., :, :, None], c[..., :, None, :]))
+
+
+def _static_corr_scale(a):
+    x = np.asarray(a, dtype=np.float64)  # (..., V, n_obs)
+    with np.errstate(invalid="ignore"):
+        c = _cond(np.nanmean(x * x, axis=-1), np.nanvar(x, axis=-1))
+    return np.fmax(1.0, np.fmax(c[..., :, None], c[..., None, :]))
+
+
 def _exp_allow(a, alpha, min_weight):
     """Pairs seen at most once (the bias is 0 mathematically, so the reference's NaN
     decision rests on rounding noise) and steps whose weight equals min_weight."""
@@ -51,7 +77,7 @@ def test_exp_matrix_vs_oracle(fname, alpha, min_weight):
     want = oracle.move_exp_matrix(fname, a, alpha=alpha, min_weight=min_weight)
     ext = oracle.move_exp_matrix(fname, a, alpha=alpha, min_weight=min_weight, ext=True)
     assert got.shape == want.shape == (2, 700, 37, 37) and got.dtype == np.float64
-    scale = _cov_scale(ext) if fname == "move_exp_nancovmatrix" else np.ones_like(ext)
+    scale = _cov_scale(ext) if fname == "move_exp_nancovmatrix" else _exp_corr_scale(a, alpha)
     r = assert_parity(got, want, ext, scale, F64_TOL, _exp_allow(a, alpha, min_weight), f"{fname} alpha={alpha}")
     assert r["allowed"] <= 0.01 * r["n"], r
 
@@ -72,7 +98,7 @@ def test_exp_matrix_float32(fname):
     assert got.dtype == np.float32
     want = oracle.move_exp_matrix(fname, a, alpha=al)
     ext = oracle.move_exp_matrix(fname, a, alpha=al, ext=True)
-    scale = _cov_scale(ext) if fname == "move_exp_nancovmatrix" else np.ones_like(ext)
+    scale = _cov_scale(ext) if fname == "move_exp_nancovmatrix" else _exp_corr_scale(a, 0.1)
     assert_parity(got, want, ext, scale, 1e-4, _exp_allow(a, 0.1, 0.0), f"{fname} float32")
 
 
@@ -109,7 +135,7 @@ def test_static_matrix_vs_oracle(fname, dtype, shape):
     want = oracle.static_matrix(fname, a)
     ext = oracle.static_matrix(fname, a.astype(np.float64), ext=True)
     assert got.shape == want.shape and got.dtype == want.dtype == dtype
-    scale = _cov_scale(ext) if fname == "nancovmatrix" else np.ones_like(ext)
+    scale = _cov_scale(ext) if fname == "nancovmatrix" else _static_corr_scale(a)
     # float32: the reference sums observations one by one in float32; this sums slices
     # of them in float32 and folds the slices, so both carry float32 rounding
     tol = F64_TOL if dtype == np.float64 else 2e-4
