@@ -516,6 +516,8 @@ def run_configs(nb, device, args):
             "fp32c_ms": per_func[base + "_fp32c"]["ms"],
             "max_rel_err_plain": per_func[base].get("max_rel_err_vs_exact"),
             "max_rel_err_fp32c": per_func[base + "_fp32c"].get("max_rel_err_vs_exact"),
+            "max_scaled_err_plain": per_func[base].get("max_scaled_err_vs_exact"),
+            "max_scaled_err_fp32c": per_func[base + "_fp32c"].get("max_scaled_err_vs_exact"),
         }
     fp32c["ragged_mix"] = {
         "speedup": round(ragged["f64"]["ms_per_mix"] / ragged["fp32c"]["ms_per_mix"], 2),
@@ -724,21 +726,23 @@ def measure_scan(nb, device, cols, steps, warmup, only=None, errors=True, error_
         entry = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 4), "Gelem/s": round(elems / ms / 1e6, 2)}
         if errors and not key.startswith(("move_covmatrix", "move_corrmatrix")):
             res = fn(nb, a[:error_rows], b[:error_rows], small, X)
-            errs = []
+            errs, serrs = [], []
             for r in range(min(error_rows, res.shape[0])):
                 pos = _sample_positions(cols, error_positions, device)
                 base = key[: -len("_fp32c")] if key.endswith("_fp32c") else key
                 if base.startswith("move_exp_"):
                     fname, al = base.rsplit("_a", 1)
-                    exact = exact_move_exp(fname, a[r], b[r] if "corr" in fname else None, float(al), pos)
+                    exact, scale = exact_move_exp(fname, a[r], b[r] if "corr" in fname else None, float(al), pos)
                 else:
                     fname, w = base.rsplit("_w", 1)
                     w = int(w)
-                    exact = exact_move(fname, a[r], b[r] if fname == "move_corr" else None, w, w // 2, pos)
-                e = max_rel_err(res[r][pos], exact)
+                    exact, scale = exact_move(fname, a[r], b[r] if fname == "move_corr" else None, w, w // 2, pos)
+                e, se = max_errors(res[r][pos], exact, scale)
                 if e is not None:
                     errs.append(e)
+                    serrs.append(se)
             entry["max_rel_err_vs_exact"] = float(f"{max(errs):.3g}") if errs else None
+            entry["max_scaled_err_vs_exact"] = float(f"{max(serrs):.3g}") if serrs else None
         per_func[key] = entry
     # the 100 x 10,000 move_mean (16 MB, resident in L2): replayed from a CUDA graph
     if not only or re.search(only, "move_mean_small"):
@@ -785,9 +789,10 @@ def scan_config(cols):
         "scan": f"{SCAN_ROWS}x{cols} float64, a = 1e6 + z1, b = 1e6 + 0.7 z1 + sqrt(0.51) z2, 2% NaN; min_count = window // 2",
         "matrix": f"{MATRIX_T}x{MATRIX_V} float32 from N(0, A A^T / 256), 1% NaN, window 500, min_count 400",
         "small": f"{SMALL_ROWS}x{SMALL_COLS} float64 N(0,1), 10% NaN, window 20, min_count 20",
-        "errors": "max |got - exact| / |exact| at 2048 evenly spaced positions of each of the first 2 rows; exact = "
-        "two-pass float64 sums of the data minus 1e6 (exact by Sterbenz) over each window, or over the weights "
-        "(1 - alpha)^k down to 1e-20",
+        "errors": "at 2048 evenly spaced positions of each of the first 2 rows: max |got - exact| / |exact| "
+        "(relative) and max |got - exact| / max(|exact|, S) (scaled; S = 1 for correlations, the mean square of "
+        "the data minus 1e6 for variances, its root for standard deviations); exact = two-pass float64 sums of "
+        "the data minus 1e6 (exact by Sterbenz) over each window, or over the weights (1 - alpha)^k down to 1e-20",
     }
 
 
@@ -858,12 +863,13 @@ def exact_move(fname, a_row, b_row, window, min_count, pos):
     if b_row is None:
         var = (da * da).sum(1) / (n - 1)
         res = torch.sqrt(var)
-        return torch.where(n >= max(min_count, 2), res, float("nan"))
+        scale = torch.sqrt((za * za).sum(1) / n)  # the root mean square of the window
+        return torch.where(n >= max(min_count, 2), res, float("nan")), scale
     zb = torch.where(valid, zb, 0.0)
     mb = zb.sum(1) / n
     db = torch.where(valid, zb - mb[:, None], 0.0)
     res = (da * db).sum(1) / torch.sqrt((da * da).sum(1) * (db * db).sum(1))
-    return torch.where(n >= max(min_count, 1), res, float("nan"))
+    return torch.where(n >= max(min_count, 1), res, float("nan")), torch.ones_like(res)
 
 
 def exact_move_exp(fname, a_row, b_row, alpha, pos):
@@ -873,6 +879,7 @@ def exact_move_exp(fname, a_row, b_row, alpha, pos):
 
     L = int(min(math.ceil(math.log(1e-20) / math.log1p(-alpha)), 1 << 22)) if alpha < 1 else 1
     out = torch.empty(pos.shape, dtype=torch.float64, device=pos.device)
+    scale = torch.empty(pos.shape, dtype=torch.float64, device=pos.device)
     step = max(1, (1 << 24) // L)
     k = torch.arange(L, device=pos.device)
     w_all = torch.exp(k.to(torch.float64) * math.log1p(-alpha))
@@ -893,29 +900,39 @@ def exact_move_exp(fname, a_row, b_row, alpha, pos):
         ma = (w * za).sum(1) / sw
         if fname == "move_exp_nanmean":
             r = ma + PIVOT
+            sc = r.abs()
         else:
             da = torch.where(valid, za - ma[:, None], 0.0)
             bias = 1 - sw2 / (sw * sw)
             if fname == "move_exp_nanvar":
                 r = torch.where(bias > 0, (w * da * da).sum(1) / sw / bias, float("nan"))
+                sc = (w * za * za).sum(1) / sw  # the weighted mean square
             else:
                 zb = torch.where(valid, zb, 0.0)
                 mb = (w * zb).sum(1) / sw
                 db = torch.where(valid, zb - mb[:, None], 0.0)
                 r = (w * da * db).sum(1) / torch.sqrt((w * da * da).sum(1) * (w * db * db).sum(1))
                 r = torch.where(bias > 0, r, float("nan"))
+                sc = torch.ones_like(r)
         out[s0 : s0 + step] = r
-    return out
+        scale[s0 : s0 + step] = sc
+    return out, scale
 
 
-def max_rel_err(got, exact):
+def max_errors(got, exact, scale):
+    """(max |got - exact| / |exact|, max |got - exact| / max(|exact|, scale)) over the
+    positions where both are finite; the second divides by the statistic's natural
+    magnitude where the statistic itself is near zero (1 for a correlation, the mean
+    square for a variance, the root mean square for a standard deviation)."""
     import torch
 
     fin = torch.isfinite(got) & torch.isfinite(exact)
     if not bool(fin.any()):
-        return None
-    err = (got[fin] - exact[fin]).abs() / exact[fin].abs().clamp_min(1e-300)
-    return float(err.max())
+        return None, None
+    diff = (got[fin] - exact[fin]).abs()
+    rel = diff / exact[fin].abs().clamp_min(1e-300)
+    scaled = diff / torch.maximum(exact[fin].abs(), scale[fin]).clamp_min(1e-300)
+    return float(rel.max()), float(scaled.max())
 
 
 # ---- the ragged batched mix ---------------------------------------------------------------

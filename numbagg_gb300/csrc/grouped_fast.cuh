@@ -900,21 +900,34 @@ __global__ void __launch_bounds__(FT, 2) big_var_kernel(const V* __restrict__ va
 #pragma unroll
       for (int rr = 0; rr < RB; ++rr) st.s[warp][u][rr][lane] = x[u][rr];
     __syncwarp();
+    // Slots i and i + 1 go to a lane pair at once: the mom = 0 lane loads the value of
+    // slot i, its partner that of slot i + 1; each squares its own and they swap
+    // (the sum lane sends its square, the square lane its value), so every element is
+    // squared once.
 #pragma unroll
     for (int u = 0; u < U; ++u) {
 #pragma unroll
-      for (int i = 0; i < LPC; ++i) {
-        const int c = i * CPI + q;
-        const B e = st.s[warp][u][r][c];
-        const long long l = __shfl_sync(0xffffffffu, lab[u], c);
-        if (!live || l < 0 || l >= K) continue;
-        const long long a = off + l * RB;
-        if (nan_bits(e)) {
-          if (mom == 0) red_add_hint(&nanc[a], 1u, keep);
-          continue;
+      for (int i = 0; i < LPC; i += 2) {
+        const int c0 = i * CPI + q, c1 = (i + 1) * CPI + q;
+        const double own = bits_to_f64(st.s[warp][u][r][mom ? c1 : c0]);
+        const double sq = own * own;
+        const double got = __shfl_xor_sync(0xffffffffu, mom ? own : sq, 1);
+        const long long l0 = __shfl_sync(0xffffffffu, lab[u], c0);
+        const long long l1 = __shfl_sync(0xffffffffu, lab[u], c1);
+        // slot i: the value (mom 0) or its square (mom 1); slot i + 1 likewise
+        const double v0 = mom ? got : own, v1 = mom ? sq : got;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const long long l = h ? l1 : l0;
+          const double v = h ? v1 : v0;
+          if (!live || l < 0 || l >= K) continue;
+          const long long a = off + l * RB;
+          if (is_nan(v)) {  // a NaN element: NaN value and NaN square
+            if (mom == 0) red_add_hint(&nanc[a], 1u, keep);
+            continue;
+          }
+          red_add_hint(&acc[2 * a + mom], v, keep);
         }
-        const double v = bits_to_f64(e);
-        red_add_hint(&acc[2 * a + mom], mom ? v * v : v, keep);
       }
     }
     __syncwarp();
@@ -1117,9 +1130,9 @@ __global__ void ragged_fold_kernel(const MomPart* __restrict__ parts, double* __
   }
 }
 
-// accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]; for the
-// variance and standard deviation both moments are interleaved, acc1[2 t + m]
-template <int F, typename O, int RB>
+// accumulators acc[t], t = (rb * K + k) * RB + r  ->  out[(rb * RB + r) * K + k]; INTER:
+// both moments interleaved in acc1[2 t + m] (big_var_kernel)
+template <int F, typename O, int RB, bool INTER>
 __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const double* __restrict__ acc2,
                                       const unsigned* __restrict__ nanc, const unsigned* __restrict__ hist,
                                       const double* __restrict__ rcp, O* __restrict__ out, long long rows,
@@ -1131,7 +1144,7 @@ __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const dou
     const long long k = rem / RB, row = rb * RB + (rem - k * RB);
     if (row >= rows) continue;
     double s1 = 0.0, s2 = 0.0;
-    if (Need<F>::varlike) {
+    if (INTER) {
       const double2 p = reinterpret_cast<const double2*>(acc1)[t];
       s1 = p.x;
       s2 = p.y;
@@ -1331,15 +1344,18 @@ template <int F, typename V, typename L, typename O, int RB>
 int launch_big_mom(const V* values, const L* labels, O* out, long long rows, long long m, long long K, long long ddof,
                    const FastPlan& p, unsigned char*& cur, cudaStream_t s) {
   const long long slots = p.blocks * RB * K;
+  // the variance and standard deviation with few rows per block (many labels, where
+  // the L2 reductions bound the kernel) interleave both moments for big_var_kernel
+  constexpr bool INTER = Need<F>::varlike && RB <= 4;
   // variance / standard deviation: both moments interleaved in acc1 (big_var_kernel)
-  double* acc1 = carve<double>(cur, Need<F>::varlike ? 2 * slots : slots);
-  double* acc2 = carve<double>(cur, (Need<F>::s2 && !Need<F>::varlike) ? slots : 1);
+  double* acc1 = carve<double>(cur, INTER ? 2 * slots : slots);
+  double* acc2 = carve<double>(cur, (Need<F>::s2 && !INTER) ? slots : 1);
   unsigned* nanc = carve<unsigned>(cur, slots);
   unsigned* hist = carve<unsigned>(cur, K);
   double* rcp = carve<double>(cur, kRcpN + 1);
   int launches = 0;
-  if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * (Need<F>::varlike ? 16 : 8), s);
-  if (Need<F>::s2 && !Need<F>::varlike) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
+  if (Need<F>::s1) cudaMemsetAsync(acc1, 0, static_cast<size_t>(slots) * (INTER ? 16 : 8), s);
+  if (Need<F>::s2 && !INTER) cudaMemsetAsync(acc2, 0, static_cast<size_t>(slots) * 8, s);
   if (Need<F>::cnt) {
     cudaMemsetAsync(nanc, 0, static_cast<size_t>(slots) * 4, s);
     cudaMemsetAsync(hist, 0, static_cast<size_t>(K) * 4, s);
@@ -1353,13 +1369,13 @@ int launch_big_mom(const V* values, const L* labels, O* out, long long rows, lon
     }
     ++launches;
   }
-  if (Need<F>::varlike)
+  if constexpr (INTER)
     big_var_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K,
                                                                                      p.chunk_len, p.chunks, acc1, nanc);
   else
     big_mom_kernel<F, V, L, RB><<<static_cast<int>(p.blocks * p.chunks), FT, 0, s>>>(values, labels, rows, m, K,
                                                                                      p.chunk_len, p.chunks, acc1, acc2, nanc);
-  big_mom_finish_kernel<F, O, RB><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
+  big_mom_finish_kernel<F, O, RB, INTER><<<fin_grid(slots), 256, 0, s>>>(acc1, acc2, nanc, hist, rcp, out, rows, K, ddof);
   return launches + 2;
 }
 

@@ -530,6 +530,307 @@ __global__ void exp_pivot_kernel(const T* __restrict__ a, const T* __restrict__ 
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Scalar alpha over rows: one pass with decoupled look-back
+// ---------------------------------------------------------------------------------
+// With one alpha every position decays every state by the same d (d^2 for
+// sum_weight_2), so a run of k positions maps s -> d^k s + B.  A tile of 1024
+// positions: each thread folds its 8 positions from zero (one multiply-add per state
+// and position); a warp scan with the multipliers d^(8 * 2^i) and a fold over the
+// four warps give every thread the tile-relative state before its run and the tile's
+// aggregate (d^1024, B); the aggregate is published at once and the state entering
+// the tile arrives through decoupled look-back over earlier tiles of the row; each
+// thread then starts from (carry * d^(8 t) + its prefix) and replays its positions,
+// finalising each.  The input is read once, and the divisions of the finalisation
+// are float32 reciprocals corrected by one float64 step (about 2^-46 relative) in
+// the float64 arithmetic.  Deterministic: every fold has a fixed order.
+
+// a / b within about 2^-46: a float32 reciprocal of b seeds one float64 correction;
+// exponents far from 1, zeros, infinities and NaN take the IEEE division
+NBG_DEVICE double fdiv(double a, double b) {
+  const unsigned eb = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(b)) >> 52) & 0x7ffu;
+  const unsigned ea = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7ffu;
+  if (eb < 1023 - 120 || eb > 1023 + 120 || ea == 0x7ffu) return a / b;
+  const double r = static_cast<double>(__frcp_rn(__double2float_rn(b)));
+  const double q0 = a * r;
+  return fma(fma(-q0, b, a), r, q0);
+}
+// sqrt(v) within about 2^-46 the same way (a float32 reciprocal square root, one
+// float64 Newton step); v <= 0, infinities, NaN and extreme exponents take sqrt
+NBG_DEVICE double fsqrt(double v) {
+  const unsigned ev = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(v)) >> 52);
+  if (ev < 1023 - 120 || ev > 1023 + 120) return sqrt(v);  // also every negative v (sign bit set)
+  const float rf = rsqrtf(__double2float_rn(v));
+  const double y0 = v * static_cast<double>(rf);
+  return fma(fma(-y0, y0, v), static_cast<double>(0.5f * rf), y0);
+}
+
+// The reference's formulas (finalize(F64, ...)) with the fast divisions above.
+template <int OP>
+NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  if (OP == kCount) return s[1] >= min_weight ? s[0] : nan;
+  if (OP == kMean) return s[2] >= min_weight ? fdiv(s[0], s[1]) : nan;
+  if (OP == kSum) return (s[1] >= min_weight && seen) ? s[0] : nan;
+  if (OP == kVar || OP == kStd) {  // numbagg/moving_exp.py:142-156
+    const double rw = fdiv(1.0, s[2]);
+    const double m = s[1] * rw;
+    const double var_biased = fma(-m, m, s[0] * rw);
+    const double bias = 1.0 - s[3] * rw * rw;
+    if (s[4] >= min_weight && bias > 0) {
+      const double v = fdiv(var_biased, bias);
+      return OP == kStd ? fsqrt(v) : v;
+    }
+    return nan;
+  }
+  if (OP == kCov) {  // numbagg/moving_exp.py:265-273
+    const double rw = fdiv(1.0, s[3]);
+    const double cov_biased = (s[2] - s[0] * s[1] * rw) * rw;
+    const double bias = 1.0 - s[4] * rw * rw;
+    return (s[5] >= min_weight && bias > 0) ? fdiv(cov_biased, bias) : nan;
+  }
+  // kCorr, numbagg/moving_exp.py:318-335
+  const double rw = fdiv(1.0, s[3]);
+  const double cov = s[2] - s[0] * s[1] * rw;
+  const double var1 = s[6] - s[0] * s[0] * rw;
+  const double var2 = s[7] - s[1] * s[1] * rw;
+  const double bias = 1.0 - s[4] * rw * rw;
+  if (s[5] >= min_weight && bias > 0) {
+    const double den = fsqrt(var1 * var2);
+    return den > 0 ? fdiv(cov, den) : nan;
+  }
+  return nan;
+}
+template <int OP>
+NBG_DEVICE double finalize_scan(F64, const double* s, int seen, double min_weight) {
+  return finalize_fast<OP>(s, seen, min_weight);
+}
+template <int OP>
+NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double min_weight) {
+  return finalize<OP>(DF(), s, seen, min_weight);
+}
+
+template <int OP, typename N>
+struct MapOp {
+  using M = Map<Traits<OP>::NS, N>;
+  NBG_DEVICE M identity() const { return identity_map<OP, N>(); }
+  NBG_DEVICE M combine(const M& earlier, const M& later) const { return compose<OP, N>(earlier, later); }
+};
+
+template <typename N>
+NBG_DEVICE typename N::T pow_n(typename N::T x, int e) {  // x^e for e >= 0, by squaring
+  typename N::T r = N::one();
+  while (e) {
+    if (e & 1) r = N::mul(r, x);
+    x = N::mul(x, x);
+    e >>= 1;
+  }
+  return r;
+}
+
+template <int OP, typename T, typename N>
+__global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                      double alpha_scalar, double min_weight, T* __restrict__ out,
+                                                      long long rows, long long n, long long tiles_per_row,
+                                                      void* ws_base, size_t ws_bytes,
+                                                      const double* __restrict__ pivots) {
+  constexpr int NS = Traits<OP>::NS;
+  constexpr int W2 = Traits<OP>::W2;
+  constexpr bool TWO = Traits<OP>::TWO;
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  typedef typename BitsOf<T>::type B;
+  typedef typename N::T V;
+  using M = Map<NS, N>;
+  __shared__ B sx[SPAD];
+  __shared__ B sy[TWO ? SPAD : 1];
+  __shared__ V wtot[NT / 32][NS];
+  __shared__ int wseen[NT / 32];
+  __shared__ M carry_smem;
+  __shared__ long long tile_smem;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  Workspace ws = make_workspace(ws_base, ws_bytes);
+  const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
+  const long long total_tiles = rows * tiles_per_row;
+
+  // decay powers shared by every tile: d^k and (d^2)^k for the runs of this thread
+  const V al = as_num(N(), alpha_scalar);
+  const V d = N::sub(N::one(), al);
+  const V dd = N::mul(d, d);
+  const V d8 = pow_n<N>(d, KT), dd8 = pow_n<N>(dd, KT);
+  const V d_lane = pow_n<N>(d8, lane), dd_lane = pow_n<N>(dd8, lane);          // over this lane's predecessors
+  const V d_warp = pow_n<N>(pow_n<N>(d8, 32), warp), dd_warp = pow_n<N>(pow_n<N>(dd8, 32), warp);
+  const V d_start = N::mul(d_warp, d_lane), dd_start = N::mul(dd_warp, dd_lane);  // d^(8 tid)
+  const V d_tile = pow_n<N>(d8, NT), dd_tile = pow_n<N>(dd8, NT);
+
+  for (;;) {
+    if (tid == 0) tile_smem = claim_tile(ws.hdr);
+    __syncthreads();
+    const long long tile = tile_smem;
+    if (tile >= total_tiles) break;
+    const TileCoord tc = tile_coord(tile, rows);  // claimed row-interleaved
+    const long long row = tc.row, chunk = tc.chunk;
+    const long long t0 = chunk * TILE;
+    const B* ar = as_bits(a) + row * n;
+    const B* br = TWO ? as_bits(b) + row * n : nullptr;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      const long long i = t0 + p;
+      const bool in = i < n;
+      sx[spad(p)] = in ? ar[i] : nanb;
+      if (TWO) sy[spad(p)] = in ? br[i] : nanb;
+    }
+    __syncthreads();
+    V px = N::zero(), py = N::zero();
+    if (SHIFT) {
+      px = as_num(N(), pivots[2 * row]);
+      if (TWO) py = as_num(N(), pivots[2 * row + 1]);
+    }
+    const int q0 = tid * KT;
+    auto load = [&](int k, V& x, V& y, bool& valid) {
+      const int sp = spad(q0 + k);
+      const B xb = sx[sp];
+      const B yb = TWO ? sy[sp] : xb;
+      valid = !nan_bits(xb) && !(TWO && nan_bits(yb));  // positions past n hold NaN
+      x = value_as(N(), xb);
+      y = TWO ? value_as(N(), yb) : x;
+      if (SHIFT) {
+        x = N::sub(x, px);
+        if (TWO) y = N::sub(y, py);
+      }
+    };
+    // ---- this thread's run folded from zero ----
+    V s[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) s[j] = N::zero();
+    int seen = 0;
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      V x, y;
+      bool valid;
+      load(k, x, y, valid);
+      V bj[NS];
+      contributions<OP, N>(x, y, al, bj);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        const V f = (j == W2) ? dd : d;
+        s[j] = valid ? N::fma(s[j], f, bj[j]) : N::mul(s[j], f);
+      }
+      seen |= valid ? 1 : 0;
+    }
+    // ---- warp scan: S_lane = sum over lanes l' <= lane of (d^8)^(lane - l') s_l' ----
+    V f1 = d8, f2 = dd8;
+#pragma unroll
+    for (int dl = 1; dl < 32; dl <<= 1) {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        const V up = shfl_up_num(s[j], dl);
+        if (lane >= dl) s[j] = N::fma(up, (j == W2) ? f2 : f1, s[j]);
+      }
+      const int us = __shfl_up_sync(0xffffffffu, seen, dl);
+      if (lane >= dl) seen |= us;
+      f1 = N::mul(f1, f1);
+      f2 = N::mul(f2, f2);
+    }
+    // exclusive prefix within the warp
+    V e[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      e[j] = shfl_up_num(s[j], 1);
+      if (lane == 0) e[j] = N::zero();
+    }
+    int eseen = __shfl_up_sync(0xffffffffu, seen, 1);
+    if (lane == 0) eseen = 0;
+    if (lane == 31) {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) wtot[warp][j] = s[j];
+      wseen[warp] = seen;
+    }
+    __syncthreads();
+    // the warps before this one, folded in order (f1 = d^256 after the scan)
+    {
+      V w[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) w[j] = N::zero();
+      int ws_seen = 0;
+      for (int u = 0; u < warp; ++u) {
+#pragma unroll
+        for (int j = 0; j < NS; ++j) w[j] = N::fma(w[j], (j == W2) ? f2 : f1, wtot[u][j]);
+        ws_seen |= wseen[u];
+      }
+      // state before this thread's run, relative to the tile start
+#pragma unroll
+      for (int j = 0; j < NS; ++j) e[j] = N::fma(w[j], (j == W2) ? dd_lane : d_lane, e[j]);
+      eseen |= ws_seen;
+    }
+    // ---- the tile's aggregate, the look-back, the carry ----
+    if (warp == 0) {
+      M agg;
+      agg.A1 = d_tile;
+      agg.A2 = dd_tile;
+      agg.pad = 0;
+      agg.seen = 0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) agg.B[j] = N::zero();
+      if (lane == 0) {
+        for (int u = 0; u < NT / 32; ++u) {
+#pragma unroll
+          for (int j = 0; j < NS; ++j) agg.B[j] = N::fma(agg.B[j], (j == W2) ? f2 : f1, wtot[u][j]);
+          agg.seen |= wseen[u];
+        }
+      }
+      M excl = identity_map<OP, N>();
+      if (chunk == 0) {
+        if (lane == 0 && tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
+      } else {
+        if (lane == 0) publish(ws, tile, epoch, kStateAggregate, agg);
+        __syncwarp();
+        bool ok;
+        excl = warp_lookback<M>(ws, tile, chunk, rows, epoch, MapOp<OP, N>(), ok);
+        if (lane == 0) publish(ws, tile, epoch, kStatePrefix, compose<OP, N>(excl, agg));
+      }
+      if (lane == 0) carry_smem = excl;
+    }
+    __syncthreads();
+    // ---- replay from the state entering this thread's run ----
+    const M carry = carry_smem;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) s[j] = N::fma(carry.B[j], (j == W2) ? dd_start : d_start, e[j]);
+    seen = eseen | carry.seen;
+    T res[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      V x, y;
+      bool valid;
+      load(k, x, y, valid);
+      V bj[NS];
+      contributions<OP, N>(x, y, al, bj);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        const V f = (j == W2) ? dd : d;
+        s[j] = valid ? N::fma(s[j], f, bj[j]) : N::mul(s[j], f);
+      }
+      seen |= valid ? 1 : 0;
+      res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight));
+    }
+    __syncthreads();  // every thread has read its run: the stage takes the outputs
+#pragma unroll
+    for (int k = 0; k < KT; ++k)
+      sx[spad(q0 + k)] = sizeof(T) == 8 ? static_cast<B>(__double_as_longlong(static_cast<double>(res[k])))
+                                        : static_cast<B>(__float_as_uint(static_cast<float>(res[k])));
+    __syncthreads();
+    B* ob = as_bits(out) + row * n;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      if (t0 + p < n) ob[t0 + p] = sx[spad(p)];
+    }
+    __syncthreads();  // the stage is reused by the next tile
+  }
+  if (tid == 0) finish_cta(ws.hdr);
+}
+
 }  // namespace mexp
 }  // namespace nbg
 
@@ -540,10 +841,45 @@ namespace {
 
 long long exp_tiles_per_row(long long n) { return n <= 0 ? 0 : (n + TILE - 1) / TILE; }
 
-// maps and carries for `tiles` tiles, pivots and the ragged plan for `rows` series
+// maps and carries for `tiles` tiles (or the look-back workspace of the one-pass scan,
+// whichever is larger), pivots and the ragged plan for `rows` series
 size_t exp_scratch_for(long long rows, long long tiles) {
-  return 2 * static_cast<size_t>(tiles) * sizeof(Map<Traits<kCorr>::NS, F64>) + 1024 +
-         static_cast<size_t>(rows) * 16 + static_cast<size_t>(rows + 1) * 8;
+  const size_t maps = 2 * static_cast<size_t>(tiles) * sizeof(Map<Traits<kCorr>::NS, F64>);
+  const size_t lookback = workspace_bytes(tiles);
+  return (maps > lookback ? maps : lookback) + 1024 + static_cast<size_t>(rows) * 16 + static_cast<size_t>(rows + 1) * 8;
+}
+
+// One pass with decoupled look-back (scalar alpha, rows x n).  The look-back state
+// (header and one status word per tile) is cleared at the start of the call.
+template <int OP, typename T, typename N>
+int launch_exp_scan(const T* a, const T* b, double alpha_scalar, double min_weight, T* out, long long rows,
+                    long long n, void* ws, cudaStream_t s) {
+  const long long tpr = exp_tiles_per_row(n);
+  const long long tiles = rows * tpr;
+  const size_t lb = workspace_bytes(tiles);
+  double* pivots = reinterpret_cast<double*>((reinterpret_cast<size_t>(ws) + lb + 255) & ~static_cast<size_t>(255));
+  if (cudaMemsetAsync(ws, 0, 256 + static_cast<size_t>(tiles) * 8, s) != cudaSuccess) return kLaunchError;
+  int launches = 1;
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  if (SHIFT) {
+    Layout lay{nullptr, nullptr, rows, n, tpr};
+    exp_pivot_kernel<T><<<static_cast<int>((rows + 7) / 8), 256, 0, s>>>(a, Traits<OP>::TWO ? b : nullptr, lay, pivots);
+    ++launches;
+  }
+  static int per_sm = 0;  // resident CTAs per SM, from the occupancy calculator
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (per_sm == 0) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exp_scan_kernel<OP, T, N>, NT, 0);
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const long long cap = static_cast<long long>(sms) * per_sm;
+  const int grid = static_cast<int>(tiles < cap ? tiles : cap);
+  exp_scan_kernel<OP, T, N><<<grid, NT, 0, s>>>(a, b, alpha_scalar, min_weight, out, rows, n, tpr, ws, lb, pivots);
+  note_launches(launches);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 
 // offsets == nullptr: rows x n; else ragged series with `total` values in all
@@ -558,6 +894,8 @@ int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int 
   // an upper bound on the tiles: each series adds at most one partial tile
   const long long tiles = offsets ? total / TILE + rows : rows * exp_tiles_per_row(n);
   if (!ws || ws_bytes < exp_scratch_for(rows, tiles)) return kWorkspaceTooSmall;
+  if (alpha_mode == 0 && !offsets)
+    return launch_exp_scan<OP, T, N>(a, b, alpha_scalar, min_weight, out, rows, n, ws, s);
   using M = Map<Traits<OP>::NS, N>;
   static_assert(sizeof(M) <= sizeof(Map<Traits<kCorr>::NS, F64>), "8-byte numbers");
   auto up = [](size_t p) { return (p + 255) & ~static_cast<size_t>(255); };
