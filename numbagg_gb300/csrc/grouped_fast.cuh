@@ -900,34 +900,23 @@ __global__ void __launch_bounds__(FT, 2) big_var_kernel(const V* __restrict__ va
 #pragma unroll
       for (int rr = 0; rr < RB; ++rr) st.s[warp][u][rr][lane] = x[u][rr];
     __syncwarp();
-    // Slots i and i + 1 go to a lane pair at once: the mom = 0 lane loads the value of
-    // slot i, its partner that of slot i + 1; each squares its own and they swap
-    // (the sum lane sends its square, the square lane its value), so every element is
-    // squared once.
 #pragma unroll
     for (int u = 0; u < U; ++u) {
 #pragma unroll
-      for (int i = 0; i < LPC; i += 2) {
-        const int c0 = i * CPI + q, c1 = (i + 1) * CPI + q;
-        const double own = bits_to_f64(st.s[warp][u][r][mom ? c1 : c0]);
-        const double sq = own * own;
-        const double got = __shfl_xor_sync(0xffffffffu, mom ? own : sq, 1);
-        const long long l0 = __shfl_sync(0xffffffffu, lab[u], c0);
-        const long long l1 = __shfl_sync(0xffffffffu, lab[u], c1);
-        // slot i: the value (mom 0) or its square (mom 1); slot i + 1 likewise
-        const double v0 = mom ? got : own, v1 = mom ? sq : got;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const long long l = h ? l1 : l0;
-          const double v = h ? v1 : v0;
-          if (!live || l < 0 || l >= K) continue;
-          const long long a = off + l * RB;
-          if (is_nan(v)) {  // a NaN element: NaN value and NaN square
-            if (mom == 0) red_add_hint(&nanc[a], 1u, keep);
-            continue;
-          }
-          red_add_hint(&acc[2 * a + mom], v, keep);
+      for (int i = 0; i < LPC; ++i) {
+        const int c = i * CPI + q;
+        const B e = st.s[warp][u][r][c];
+        const long long l = __shfl_sync(0xffffffffu, lab[u], c);
+        if (!live || l < 0 || l >= K) continue;
+        const long long a = off + l * RB;
+        if (nan_bits(e)) {
+          if (mom == 0) red_add_hint(&nanc[a], 1u, keep);
+          continue;
         }
+        // both lanes of a pair square the element (the sum lane's square is dropped):
+        // with few rows per block the L2 reductions, not the FP64 pipe, bound this
+        const double v = bits_to_f64(e);
+        red_add_hint(&acc[2 * a + mom], mom ? v * v : v, keep);
       }
     }
     __syncwarp();

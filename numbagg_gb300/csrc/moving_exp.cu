@@ -565,7 +565,22 @@ NBG_DEVICE double fsqrt(double v) {
   return fma(fma(-y0, y0, v), static_cast<double>(0.5f * rf), y0);
 }
 
-// The reference's formulas (finalize(F64, ...)) with the fast divisions above.
+// a / b nearly correctly rounded (Markstein's sequence: the float32 reciprocal refined
+// once, then the quotient corrected once; P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+// for the quotients that feed a cancellation (the bias 1 - sw2 / sw^2 and the biased
+// variance), whose errors the subtraction amplifies
+NBG_DEVICE double mdiv(double a, double b) {
+  const unsigned eb = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(b)) >> 52) & 0x7ffu;
+  const unsigned ea = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7ffu;
+  if (eb < 1023 - 120 || eb > 1023 + 120 || ea == 0x7ffu) return a / b;
+  double r = static_cast<double>(__frcp_rn(__double2float_rn(b)));
+  r = fma(fma(-b, r, 1.0), r, r);
+  const double q0 = a * r;
+  return fma(fma(-q0, b, a), r, q0);
+}
+
+// The reference's formulas (finalize(F64, ...)), in the reference's order, with the
+// divisions above: mdiv inside, fdiv for a final quotient (not amplified further).
 template <int OP>
 NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
@@ -573,10 +588,9 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   if (OP == kMean) return s[2] >= min_weight ? fdiv(s[0], s[1]) : nan;
   if (OP == kSum) return (s[1] >= min_weight && seen) ? s[0] : nan;
   if (OP == kVar || OP == kStd) {  // numbagg/moving_exp.py:142-156
-    const double rw = fdiv(1.0, s[2]);
-    const double m = s[1] * rw;
-    const double var_biased = fma(-m, m, s[0] * rw);
-    const double bias = 1.0 - s[3] * rw * rw;
+    const double m = mdiv(s[1], s[2]);
+    const double var_biased = mdiv(s[0], s[2]) - m * m;
+    const double bias = 1.0 - mdiv(s[3], s[2] * s[2]);
     if (s[4] >= min_weight && bias > 0) {
       const double v = fdiv(var_biased, bias);
       return OP == kStd ? fsqrt(v) : v;
@@ -584,17 +598,15 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
     return nan;
   }
   if (OP == kCov) {  // numbagg/moving_exp.py:265-273
-    const double rw = fdiv(1.0, s[3]);
-    const double cov_biased = (s[2] - s[0] * s[1] * rw) * rw;
-    const double bias = 1.0 - s[4] * rw * rw;
+    const double cov_biased = fdiv(s[2] - mdiv(s[0] * s[1], s[3]), s[3]);
+    const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
     return (s[5] >= min_weight && bias > 0) ? fdiv(cov_biased, bias) : nan;
   }
   // kCorr, numbagg/moving_exp.py:318-335
-  const double rw = fdiv(1.0, s[3]);
-  const double cov = s[2] - s[0] * s[1] * rw;
-  const double var1 = s[6] - s[0] * s[0] * rw;
-  const double var2 = s[7] - s[1] * s[1] * rw;
-  const double bias = 1.0 - s[4] * rw * rw;
+  const double cov = s[2] - mdiv(s[0] * s[1], s[3]);
+  const double var1 = s[6] - mdiv(s[0] * s[0], s[3]);
+  const double var2 = s[7] - mdiv(s[1] * s[1], s[3]);
+  const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
   if (s[5] >= min_weight && bias > 0) {
     const double den = fsqrt(var1 * var2);
     return den > 0 ? fdiv(cov, den) : nan;
