@@ -613,13 +613,65 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   }
   return nan;
 }
+// Double-float finalisation of the one-pass scan: min_weight converted once per
+// kernel, comparisons on the (hi, lo) pair, and divisions as one float32 quotient plus
+// one correction (about 2^-44 relative, far inside the compensated form's bound).
+NBG_DEVICE bool df_ge_df(dfl::df x, dfl::df y) {  // x >= y for normalised pairs
+  return x.hi > y.hi || (x.hi == y.hi && x.lo >= y.lo);
+}
+NBG_DEVICE dfl::df df_div_fast(dfl::df x, dfl::df y) {
+  using namespace dfl;
+  if (y.hi == 0.0f || !isfinite(y.hi) || !isfinite(x.hi)) return df{__fdiv_rn(x.hi, y.hi), 0.0f};
+  const float r = __frcp_rn(y.hi);
+  const float q1 = __fmul_rn(x.hi, r);
+  const df e = df_sub(x, df_mul_f(y, q1));
+  return fast_two_sum(q1, __fmul_rn(e.hi, r));
+}
 template <int OP>
-NBG_DEVICE double finalize_scan(F64, const double* s, int seen, double min_weight) {
+NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
+  using namespace dfl;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const df one{1.0f, 0.0f};
+  if (OP == kCount) return df_ge_df(s[1], mw) ? df_to_f64(s[0]) : nan;
+  if (OP == kMean) return df_ge_df(s[2], mw) ? df_to_f64(df_div_fast(s[0], s[1])) : nan;
+  if (OP == kSum) return (df_ge_df(s[1], mw) && seen) ? df_to_f64(s[0]) : nan;
+  if (OP == kVar || OP == kStd) {
+    const df rw = df_div_fast(one, s[2]);
+    const df m = df_mul(s[1], rw);
+    const df var_biased = df_sub(df_mul(s[0], rw), df_mul(m, m));
+    const df bias = df_sub(one, df_mul(s[3], df_mul(rw, rw)));
+    if (df_ge_df(s[4], mw) && df_pos(bias)) {
+      const df v = df_div_fast(var_biased, bias);
+      if (OP == kVar) return df_to_f64(v);
+      if (v.hi < 0.0f) return nan;
+      return v.hi == 0.0f ? 0.0 : df_to_f64(df_sqrt(v));
+    }
+    return nan;
+  }
+  const df rw = df_div_fast(one, s[3]);
+  const df bias = df_sub(one, df_mul(s[4], df_mul(rw, rw)));
+  if (OP == kCov) {
+    const df cov_biased = df_mul(df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw)), rw);
+    return (df_ge_df(s[5], mw) && df_pos(bias)) ? df_to_f64(df_div_fast(cov_biased, bias)) : nan;
+  }
+  const df cov = df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw));
+  const df var1 = df_sub(s[6], df_mul(df_mul(s[0], s[0]), rw));
+  const df var2 = df_sub(s[7], df_mul(df_mul(s[1], s[1]), rw));
+  if (df_ge_df(s[5], mw) && df_pos(bias)) {
+    const df vv = df_mul(var1, var2);
+    if (!df_pos(vv)) return nan;
+    return df_to_f64(df_div_fast(cov, df_sqrt(vv)));
+  }
+  return nan;
+}
+
+template <int OP>
+NBG_DEVICE double finalize_scan(F64, const double* s, int seen, double min_weight, double) {
   return finalize_fast<OP>(s, seen, min_weight);
 }
 template <int OP>
-NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double min_weight) {
-  return finalize<OP>(DF(), s, seen, min_weight);
+NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double, dfl::df mw) {
+  return finalize_dfast<OP>(s, seen, mw);
 }
 
 template <int OP, typename N>
@@ -665,6 +717,7 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
   const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
   const long long total_tiles = rows * tiles_per_row;
 
+  const V mw_n = as_num(N(), min_weight);  // min_weight in the policy's numbers, once
   // decay powers shared by every tile: d^k and (d^2)^k for the runs of this thread
   const V al = as_num(N(), alpha_scalar);
   const V d = N::sub(N::one(), al);
@@ -726,8 +779,10 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
       contributions<OP, N>(x, y, al, bj);
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
-        const V f = (j == W2) ? dd : d;
-        s[j] = valid ? N::fma(s[j], f, bj[j]) : N::mul(s[j], f);
+        // a missing value contributes zero: one multiply-add either way (s * f + 0
+        // rounds like the product alone)
+        if (!valid) bj[j] = N::zero();
+        s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
       }
       seen |= valid ? 1 : 0;
     }
@@ -820,11 +875,13 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
       contributions<OP, N>(x, y, al, bj);
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
-        const V f = (j == W2) ? dd : d;
-        s[j] = valid ? N::fma(s[j], f, bj[j]) : N::mul(s[j], f);
+        // a missing value contributes zero: one multiply-add either way (s * f + 0
+        // rounds like the product alone)
+        if (!valid) bj[j] = N::zero();
+        s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
       }
       seen |= valid ? 1 : 0;
-      res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight));
+      res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight, mw_n));
     }
     __syncthreads();  // every thread has read its run: the stage takes the outputs
 #pragma unroll
