@@ -67,7 +67,7 @@ def parse_args(argv=None):
         "ragged: the batched mix of series of uneven length; link: pinned host<->device copy "
         "bandwidth (the bound of the end-to-end number); aggregate: the static aggregations",
     )
-    p.add_argument("--ragged-series", type=int, default=20_000, help="series in the ragged batch")
+    p.add_argument("--ragged-series", type=int, default=100_000, help="series in the ragged batch")
     p.add_argument(
         "--no-configs",
         action="store_true",
@@ -938,11 +938,18 @@ def max_errors(got, exact, scale):
 # ---- the ragged batched mix ---------------------------------------------------------------
 
 
-def measure_ragged(nb, device, nseries, steps, warmup):
+RAGGED_SLICE_ELEMS = 2_500_000_000  # elements per streamed slice of series (outputs sized for one slice)
+
+
+def measure_ragged(nb, device, nseries, steps, warmup, slice_elems=RAGGED_SLICE_ELEMS):
     """Series with lengths log-uniform in [16, 10^6] (seeded), N(0,1) with 3% NaN, int32
     labels uniform in [0, 64), flat float64 buffer plus int64 offsets; every series runs
-    move_mean(window=20), move_exp_nanstd(alpha=0.05) and group_nanmean(64 labels), as one
-    captured CUDA graph (RaggedMix, chunk length autotuned), plain float64 and fp32c."""
+    move_mean(window=20), move_exp_nanstd(alpha=0.05) and group_nanmean(64 labels).
+    The batch is resident in HBM; it is cut into slices of consecutive series of at most
+    `slice_elems` elements, each slice one captured CUDA graph (RaggedMix, chunk length
+    autotuned) writing into one pair of output buffers sized for the largest slice, so
+    the 100,000-series batch (about 9e9 values, 108 GB of inputs) streams through about
+    40 GB of outputs.  A step replays every slice's graph; plain float64 and fp32c."""
     import numpy as np
     import torch
 
@@ -954,22 +961,49 @@ def measure_ragged(nb, device, nseries, steps, warmup):
     total = int(offsets_np[-1])
     g = torch.Generator(device=device)
     g.manual_seed(5)
-    values = torch.randn(total, generator=g, dtype=torch.float64, device=device)
-    values[torch.rand(total, generator=g, device=device) < 0.03] = float("nan")
-    labels = torch.randint(0, 64, (total,), generator=g, dtype=torch.int32, device=device)
+    values = torch.empty(total, dtype=torch.float64, device=device)
+    labels = torch.empty(total, dtype=torch.int32, device=device)
+    piece = 1 << 28
+    for p0 in range(0, total, piece):  # generated in pieces to bound the temporaries
+        p1 = min(total, p0 + piece)
+        v = torch.randn(p1 - p0, generator=g, dtype=torch.float64, device=device)
+        v[torch.rand(p1 - p0, generator=g, device=device) < 0.03] = float("nan")
+        values[p0:p1] = v
+        labels[p0:p1] = torch.randint(0, 64, (p1 - p0,), generator=g, dtype=torch.int32, device=device)
+        del v
     offsets = torch.from_numpy(offsets_np).to(device)
+    # slices of consecutive series
+    bounds, s0 = [], 0
+    while s0 < nseries:
+        s1 = s0 + 1
+        while s1 < nseries and offsets_np[s1 + 1] - offsets_np[s0] <= slice_elems:
+            s1 += 1
+        bounds.append((s0, s1))
+        s0 = s1
+    longest = max(int(offsets_np[b] - offsets_np[a]) for a, b in bounds)
+    mean_buf = torch.empty(longest, dtype=torch.float64, device=device)
+    std_buf = torch.empty(longest, dtype=torch.float64, device=device)
     stream = torch.cuda.current_stream(device)
     res = {}
     launches0 = _lib.launch_count()
     for precision in ("f64", "fp32c"):
-        mix = nb.ragged.RaggedMix(values, labels, offsets, window=20, alpha=0.05, num_labels=64, precision=precision)
+        mixes = []
+        for a, b in bounds:
+            e0, e1 = int(offsets_np[a]), int(offsets_np[b])
+            mixes.append(
+                nb.ragged.RaggedMix(values[e0:e1], labels[e0:e1], offsets[a : b + 1] - offsets[a], window=20,
+                                    alpha=0.05, num_labels=64, precision=precision,
+                                    outs=[mean_buf[: e1 - e0], std_buf[: e1 - e0], None])
+            )
         for _ in range(warmup):
-            mix.run()
+            for mix in mixes:
+                mix.run()
         torch.cuda.synchronize(device)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            mix.run()
+            for mix in mixes:
+                mix.run()
         e1.record(stream)
         torch.cuda.synchronize(device)
         ms = e0.elapsed_time(e1) / steps
@@ -977,16 +1011,19 @@ def measure_ragged(nb, device, nseries, steps, warmup):
             "ms_per_mix": round(ms, 3),
             "elements_per_s": round(total / (ms / 1e3), 1),
             "GB/s": round((8 + 4 + 8 + 8) * total / (ms / 1e3) / 1e9, 1),
-            "chunk_len": mix.chunk,
+            "chunk_len": sorted({m.chunk for m in mixes}),
+            "graphs_per_step": len(mixes),
         }
-        del mix
-    del values, labels, offsets
+        del mixes
+    del values, labels, offsets, mean_buf, std_buf
     torch.cuda.empty_cache()
     config = {
         "series": nseries,
         "elements": total,
         "lengths": "round(exp(U(ln 16, ln 1e6))), seed 5",
         "values": "float64 N(0,1), 3% NaN; int32 labels U[0, 64)",
+        "streaming": f"{len(bounds)} slices of consecutive series, at most {slice_elems} elements each, one "
+        "captured graph per slice, outputs in one pair of buffers sized for the largest slice",
     }
     return res, config, int(_lib.launch_count() - launches0)
 

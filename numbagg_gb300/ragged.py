@@ -16,9 +16,11 @@ numbagg function of the same name computes on every series on its own:
 Every scan also takes ``precision="fp32c"`` (the FP32-compensated forms).  The kernels
 walk the series with one persistent grid; the work items are planned on the device,
 so the calls contain no host round trip and can be captured in a CUDA graph.
-``RaggedMix`` captures a whole pipeline (moving mean, EWM standard deviation and a
-grouped mean per series) as one graph and replays it, with the chunk length chosen by
-``autotune`` and cached per shape.
+``RaggedPlan`` captures any list of requests (function, window / alpha / num_labels)
+over one batch as a single CUDA graph and replays it, each moving-window chunk length
+chosen by ``autotune_chunk`` and cached per shape and GPU model; ``RaggedMix`` is the
+plan of the benchmark's pipeline (moving mean, EWM standard deviation and a grouped
+mean per series).
 """
 
 from __future__ import annotations
@@ -176,36 +178,56 @@ _cache_lock = threading.Lock()
 _CACHE_FILE = os.environ.get("NUMBAGG_GB300_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "numbagg_gb300_tune.json"))
 
 
-def _shape_key(op, precision, nseries, total, window):
-    # shapes in the same power-of-two buckets share a choice
-    return f"{op}|{precision}|s{int(math.log2(max(nseries, 1)))}|n{int(math.log2(max(total, 1)))}|w{window}"
+def device_key(device) -> str:
+    """The GPU a tuned choice belongs to: its name, SM count and compute capability."""
+    p = torch.cuda.get_device_properties(device)
+    return f"{p.name}|sm{p.multi_processor_count}|cc{p.major}{p.minor}".replace(" ", "_")
 
 
-def _load_cache():
+def _shape_key(op, precision, nseries, total, window, dev="any"):
+    # shapes in the same power-of-two buckets share a choice, per GPU model
+    return f"{dev}|{op}|{precision}|s{int(math.log2(max(nseries, 1)))}|n{int(math.log2(max(total, 1)))}|w{window}"
+
+
+def _read_cache_file() -> dict[str, int]:
     try:
         with open(_CACHE_FILE) as fh:
             data = json.load(fh)
         if isinstance(data, dict):
-            _cache.update({str(k): int(v) for k, v in data.items()})
-    except (OSError, ValueError):
+            return {str(k): int(v) for k, v in data.items()}
+    except (OSError, ValueError, TypeError):
         pass
+    return {}
+
+
+def _load_cache():
+    _cache.update(_read_cache_file())
 
 
 def _save_cache():
+    """Merge this process's choices into the file and replace it atomically (a temporary
+    file in the same directory, then os.replace), so concurrent processes never read a
+    half-written cache."""
     try:
-        os.makedirs(os.path.dirname(_CACHE_FILE), exist_ok=True)
-        with open(_CACHE_FILE, "w") as fh:
-            json.dump(_cache, fh, indent=1, sort_keys=True)
+        d = os.path.dirname(_CACHE_FILE) or "."
+        os.makedirs(d, exist_ok=True)
+        merged = _read_cache_file()
+        merged.update(_cache)
+        tmp = f"{_CACHE_FILE}.{os.getpid()}.{threading.get_ident()}.tmp"
+        with open(tmp, "w") as fh:
+            json.dump(merged, fh, indent=1, sort_keys=True)
+        os.replace(tmp, _CACHE_FILE)
     except OSError:
         pass
 
 
 def autotune_chunk(op, values, offsets, *, window, precision="f64", reps=3):
     """Chunk length (positions per work item) of the ragged moving-window kernel for this
-    shape: each candidate is timed with CUDA events on the real batch, the fastest is
-    kept in a process-wide cache (also written to a JSON file, NUMBAGG_GB300_TUNE_CACHE
-    or ~/.cache/numbagg_gb300_tune.json, and read back by later processes)."""
-    key = _shape_key(op, precision, offsets.numel() - 1, values.numel(), window)
+    shape on this GPU: each candidate is timed with CUDA events on the real batch, the
+    fastest is kept in a process-wide cache (also merged into a JSON file,
+    NUMBAGG_GB300_TUNE_CACHE or ~/.cache/numbagg_gb300_tune.json, keyed by the GPU
+    model, and read back by later processes)."""
+    key = _shape_key(op, precision, offsets.numel() - 1, values.numel(), window, device_key(values.device))
     with _cache_lock:
         if not _cache:
             _load_cache()
@@ -231,24 +253,74 @@ def autotune_chunk(op, values, offsets, *, window, precision="f64", reps=3):
     return best
 
 
-class RaggedMix:
-    """One pipeline over a ragged batch -- move_mean(window), move_exp_nanstd(alpha) and
-    group_nanmean(num_labels) of every series -- captured once as a CUDA graph and
-    replayed by ``run()``.  Inputs are read from the tensors given here (refill them in
-    place between runs); outputs are preallocated and returned by ``run()``."""
+# ---- one graph over many requests ----------------------------------------------------
 
-    def __init__(self, values, labels, offsets, *, window=20, alpha=0.05, num_labels=64, precision="f64",
-                 tune=True):
+MOVE_OPS = ("move_sum", "move_mean", "move_var", "move_std")
+EXP_OPS = ("move_exp_nanmean", "move_exp_nanvar", "move_exp_nanstd")
+GROUP_OPS = ("group_nansum", "group_nanmean", "group_nancount")
+
+
+def check_request(name, params):
+    """(name, parameters) of one request; raises for unknown functions or keywords."""
+    allowed = {
+        **{op: {"window", "min_count"} for op in MOVE_OPS},
+        **{op: {"alpha", "min_weight"} for op in EXP_OPS},
+        **{op: {"num_labels"} for op in GROUP_OPS},
+    }
+    if name not in allowed:
+        raise ValueError(f"unknown ragged function {name!r}; one of {sorted(allowed)}")
+    extra = set(params) - allowed[name]
+    if extra:
+        raise TypeError(f"{name} got unexpected keywords {sorted(extra)}")
+    needed = {"window"} if name in MOVE_OPS else ({"alpha"} if name in EXP_OPS else {"num_labels"})
+    missing = needed - set(params)
+    if missing:
+        raise TypeError(f"{name} needs {sorted(missing)}")
+    return name, dict(params)
+
+
+class RaggedPlan:
+    """Many requests -- any mix of the moving-window, exponentially weighted and grouped
+    functions above, each with its own window / alpha / num_labels -- over one ragged
+    batch, captured once as a single CUDA graph and replayed by ``run()``.
+
+    ``requests`` is a list of ``(name, params)``, e.g. ``[("move_mean", {"window": 20}),
+    ("move_exp_nanstd", {"alpha": 0.05}), ("group_nanmean", {"num_labels": 64})]``.
+    Every moving-window request's chunk length is autotuned for this shape on this GPU
+    (``tune=False``: the kernels' default).  Inputs are read from the tensors given here
+    (refill them in place between runs).  ``outs`` may hold a preallocated output per
+    request (None: allocate), so that plans over successive slices of a larger batch
+    can share output buffers; ``run()`` returns the outputs in request order."""
+
+    def __init__(self, values, offsets, requests, *, labels=None, precision="f64", tune=True, outs=None):
         check_offsets(values, offsets)
-        self.values, self.offsets = values, offsets
-        self.labels = labels
-        self.window, self.alpha, self.num_labels, self.precision = window, alpha, num_labels, precision
+        _sfx(precision)
+        self.values, self.offsets, self.labels, self.precision = values, offsets, labels, precision
+        self.requests = [check_request(n, p) for n, p in requests]
+        if any(n in GROUP_OPS for n, _ in self.requests) and labels is None:
+            raise TypeError("grouped requests need labels laid out like values")
         dev = values.device
         nseries = offsets.numel() - 1
-        self.chunk = autotune_chunk("move_mean", values, offsets, window=window, precision=precision) if tune else 0
-        self.mean = torch.empty_like(values)
-        self.std = torch.empty_like(values)
-        self.groups = torch.empty((nseries, num_labels), dtype=torch.float64, device=dev)
+        outs = list(outs) if outs is not None else [None] * len(self.requests)
+        if len(outs) != len(self.requests):
+            raise ValueError("outs needs one entry per request")
+        self.chunks, self.outs = [], []
+        for (name, p), o in zip(self.requests, outs):
+            if name in MOVE_OPS:
+                c = autotune_chunk(name, values, offsets, window=p["window"], precision=precision) if tune else 0
+                o = torch.empty_like(values) if o is None else o
+            elif name in EXP_OPS:
+                c = 0
+                o = torch.empty_like(values) if o is None else o
+            else:
+                c = 0
+                shape = (nseries, p["num_labels"])
+                o = torch.empty(shape, dtype=torch.float64, device=dev) if o is None else o
+            want = values.shape if name not in GROUP_OPS else (nseries, p["num_labels"])
+            if tuple(o.shape) != tuple(want) or o.dtype != torch.float64 or o.device != dev:
+                raise ValueError(f"output for {name} must be float64 {tuple(want)} on {dev}")
+            self.chunks.append(c)
+            self.outs.append(o)
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -258,12 +330,41 @@ class RaggedMix:
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph, stream=side):
             self._body()
-        self.launches_per_run = None
 
     def _body(self):
-        _move("move_mean", self.values, self.offsets, self.window, None, self.precision, self.chunk, self.mean)
-        _move_exp("move_exp_nanstd", self.values, self.offsets, self.alpha, 0, self.precision, self.std)
-        _group("nanmean", self.values, self.labels, self.offsets, self.num_labels, self.groups)
+        for (name, p), c, o in zip(self.requests, self.chunks, self.outs):
+            if name in MOVE_OPS:
+                _move(name, self.values, self.offsets, p["window"], p.get("min_count"), self.precision, c, o)
+            elif name in EXP_OPS:
+                _move_exp(name, self.values, self.offsets, p["alpha"], p.get("min_weight", 0), self.precision, o)
+            else:
+                _group(name[len("group_"):], self.values, self.labels, self.offsets, p["num_labels"], o)
+
+    def run(self):
+        self.graph.replay()
+        return self.outs
+
+
+class RaggedMix(RaggedPlan):
+    """The benchmark's pipeline as a RaggedPlan: move_mean(window), move_exp_nanstd(alpha)
+    and group_nanmean(num_labels) of every series.  ``run()`` returns (mean, std,
+    groups)."""
+
+    def __init__(self, values, labels, offsets, *, window=20, alpha=0.05, num_labels=64, precision="f64",
+                 tune=True, outs=None):
+        super().__init__(
+            values,
+            offsets,
+            [("move_mean", {"window": window}), ("move_exp_nanstd", {"alpha": alpha}),
+             ("group_nanmean", {"num_labels": num_labels})],
+            labels=labels,
+            precision=precision,
+            tune=tune,
+            outs=outs,
+        )
+        self.window, self.alpha, self.num_labels = window, alpha, num_labels
+        self.chunk = self.chunks[0]
+        self.mean, self.std, self.groups = self.outs
 
     def run(self):
         self.graph.replay()
@@ -272,8 +373,11 @@ class RaggedMix:
 
 __all__ = [
     "RaggedMix",
+    "RaggedPlan",
     "autotune_chunk",
     "check_offsets",
+    "check_request",
+    "device_key",
     "group_nancount",
     "group_nanmean",
     "group_nansum",

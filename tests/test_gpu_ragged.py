@@ -107,3 +107,56 @@ def test_ragged_mix_graph_replays_the_direct_calls():
     mean2, _, _ = mix.run()
     torch.cuda.synchronize()
     assert torch.equal(torch.nan_to_num(mean2, nan=9.0), torch.nan_to_num(nb.ragged.move_mean(v, o, window=20), nan=9.0))
+
+
+def _eq(a, b):
+    return torch.equal(torch.nan_to_num(a, nan=9.0), torch.nan_to_num(b, nan=9.0))
+
+
+def test_ragged_plan_many_requests_one_graph():
+    values, labels, offsets = _batch(45, nseries=200, max_len=20000)
+    v, lab, o = _dev(values, labels, offsets)
+    requests = [
+        ("move_mean", {"window": 20}),
+        ("move_std", {"window": 252, "min_count": 100}),
+        ("move_exp_nanmean", {"alpha": 0.3}),
+        ("move_exp_nanstd", {"alpha": 0.05}),
+        ("group_nansum", {"num_labels": 70}),
+        ("group_nancount", {"num_labels": 16}),
+    ]
+    for precision in ("f64", "fp32c"):
+        plan = nb.ragged.RaggedPlan(v, o, requests, labels=lab, precision=precision)
+        outs = plan.run()
+        torch.cuda.synchronize()
+        assert _eq(outs[0], nb.ragged.move_mean(v, o, window=20, precision=precision))
+        assert _eq(outs[1], nb.ragged.move_std(v, o, window=252, min_count=100, precision=precision))
+        assert _eq(outs[2], nb.ragged.move_exp_nanmean(v, o, alpha=0.3, precision=precision))
+        assert _eq(outs[3], nb.ragged.move_exp_nanstd(v, o, alpha=0.05, precision=precision))
+        assert _eq(outs[4], nb.ragged.group_nansum(v, lab, o, num_labels=70))
+        assert _eq(outs[5], nb.ragged.group_nancount(v, lab, o, num_labels=16))
+
+
+def test_ragged_plans_over_slices_share_outputs():
+    # a batch cut into two slices of series, each its own plan writing into views of one
+    # pair of output buffers (how a batch larger than the device's room is streamed)
+    values, labels, offsets = _batch(46, nseries=120, max_len=20000)
+    v, lab, o = _dev(values, labels, offsets)
+    longest = max(int(offsets[60] - offsets[0]), int(offsets[120] - offsets[60]))
+    mean_buf = torch.empty(longest, dtype=torch.float64, device="cuda")
+    std_buf = torch.empty_like(mean_buf)
+    results = []
+    for s0, s1 in ((0, 60), (60, 120)):
+        e0, e1 = int(offsets[s0]), int(offsets[s1])
+        vo = v[e0:e1]
+        oo = o[s0 : s1 + 1] - o[s0]
+        mix = nb.ragged.RaggedMix(vo, lab[e0:e1], oo, window=20, alpha=0.05, num_labels=70,
+                                  outs=[mean_buf[: e1 - e0], std_buf[: e1 - e0], None])
+        mean, std, groups = mix.run()
+        torch.cuda.synchronize()
+        results.append((mean.clone(), std.clone(), groups.clone()))
+    full_mean = nb.ragged.move_mean(v, o, window=20)
+    full_std = nb.ragged.move_exp_nanstd(v, o, alpha=0.05)
+    full_groups = nb.ragged.group_nanmean(v, lab, o, num_labels=70)
+    assert _eq(torch.cat([results[0][0], results[1][0]]), full_mean)
+    assert _eq(torch.cat([results[0][1], results[1][1]]), full_std)
+    assert _eq(torch.cat([results[0][2], results[1][2]]), full_groups)

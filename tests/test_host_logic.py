@@ -41,11 +41,13 @@ def test_ragged_precision_keyword():
 
 
 def test_autotune_shape_buckets():
-    k = ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 20)
-    assert k == ragged._shape_key("move_mean", "f64", 30_000, 2_000_000_000, 20)  # same power-of-two buckets
-    assert k != ragged._shape_key("move_mean", "f64", 40_000, 2_000_000_000, 20)
-    assert k != ragged._shape_key("move_mean", "fp32c", 20_000, 1_830_000_000, 20)
-    assert k != ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 21)
+    k = ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 20, "GB300|sm152|cc103")
+    assert k == ragged._shape_key("move_mean", "f64", 30_000, 2_000_000_000, 20, "GB300|sm152|cc103")  # same buckets
+    assert k != ragged._shape_key("move_mean", "f64", 40_000, 2_000_000_000, 20, "GB300|sm152|cc103")
+    assert k != ragged._shape_key("move_mean", "fp32c", 20_000, 1_830_000_000, 20, "GB300|sm152|cc103")
+    assert k != ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 21, "GB300|sm152|cc103")
+    # a choice made on one GPU model is not reused on another
+    assert k != ragged._shape_key("move_mean", "f64", 20_000, 1_830_000_000, 20, "B200|sm148|cc100")
 
 
 def test_autotune_cache_round_trip(tmp_path, monkeypatch):
@@ -57,10 +59,25 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
     monkeypatch.setattr(ragged, "_cache", {})
     ragged._load_cache()
     assert ragged._cache == {"move_mean|f64|s14|n30|w20": 32768}
+    # a save merges with what other processes wrote meanwhile, and leaves no temporary
+    path.write_text(json.dumps({"other|key": 8192, "move_mean|f64|s14|n30|w20": 1}))
+    ragged._save_cache()
+    assert json.loads(path.read_text()) == {"other|key": 8192, "move_mean|f64|s14|n30|w20": 32768}
+    assert sorted(p.name for p in tmp_path.iterdir()) == ["tune.json"]
     path.write_text("not json")
     monkeypatch.setattr(ragged, "_cache", {})
     ragged._load_cache()  # a corrupt file is ignored
     assert ragged._cache == {}
+
+
+def test_ragged_requests_are_checked():
+    assert ragged.check_request("move_mean", {"window": 20}) == ("move_mean", {"window": 20})
+    with pytest.raises(ValueError, match="unknown ragged function"):
+        ragged.check_request("move_median", {"window": 3})
+    with pytest.raises(TypeError, match="unexpected keywords"):
+        ragged.check_request("move_exp_nanmean", {"alpha": 0.1, "window": 3})
+    with pytest.raises(TypeError, match="needs"):
+        ragged.check_request("group_nanmean", {})
 
 
 # ---- bench --------------------------------------------------------------------------------
