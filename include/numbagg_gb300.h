@@ -162,6 +162,32 @@ NBG_DECL_EXP1(move_exp_nanstd, double, f64_fp32c)
 NBG_DECL_EXP2(move_exp_nancov, double, f64_fp32c)
 NBG_DECL_EXP2(move_exp_nancorr, double, f64_fp32c)
 
+/* The exponentially weighted family along a non-last axis of C-contiguous arrays, as the
+ * fills above (numbagg/decorators.py:409-414 hands the gufunc the strided axis): `outer`
+ * blocks of n x `inner` values scanned along n, one thread per column running numbagg's
+ * loop (the float64 arithmetic repeats the reference's operations in order).
+ * alpha_mode 0: scalar; 1: n values along the axis; 2: one per element, laid out like a.
+ * No workspace. */
+#define NBG_DECL_EXP1_COLS(NAME, T, SFX)                                                              \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, const T* alpha, double alpha_scalar, int alpha_mode, \
+                                      double min_weight, T* out, long long outer, long long n,         \
+                                      long long inner, void* stream);
+#define NBG_DECL_EXP2_COLS(NAME, T, SFX)                                                              \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,     \
+                                      int alpha_mode, double min_weight, T* out, long long outer,      \
+                                      long long n, long long inner, void* stream);
+#define NBG_DECL_EXP_COLS_ALL(T, SFX)                \
+  NBG_DECL_EXP1_COLS(move_exp_nancount, T, SFX)      \
+  NBG_DECL_EXP1_COLS(move_exp_nanmean, T, SFX)       \
+  NBG_DECL_EXP1_COLS(move_exp_nansum, T, SFX)        \
+  NBG_DECL_EXP1_COLS(move_exp_nanvar, T, SFX)        \
+  NBG_DECL_EXP1_COLS(move_exp_nanstd, T, SFX)        \
+  NBG_DECL_EXP2_COLS(move_exp_nancov, T, SFX)        \
+  NBG_DECL_EXP2_COLS(move_exp_nancorr, T, SFX)
+NBG_DECL_EXP_COLS_ALL(double, f64)
+NBG_DECL_EXP_COLS_ALL(float, f32)
+NBG_DECL_EXP_COLS_ALL(double, f64_fp32c)
+
 /* Ragged batches of exponentially weighted functions (no reference counterpart):
  * series as for the moving windows, `total` = offsets[nseries]; alpha_mode 0 (scalar
  * alpha_scalar) or 2 (one alpha per value, laid out like values).  ws:
@@ -194,6 +220,21 @@ NBG_DECL_FILL(double, f64)
 NBG_DECL_FILL(float, f32)
 NBG_DECL_FILL(int, i32)
 NBG_DECL_FILL(long long, i64)
+
+/* Fills along a non-last axis of a C-contiguous array, in place of moving the axis last
+ * and copying (numbagg's gufuncs take such strided core axes directly,
+ * numbagg/decorators.py:340-341, :480-487): `outer` blocks of n x `inner` values, position
+ * p of column i of block o at a[(o * n + p) * inner + i]; out laid out like a.  One
+ * thread per column, no workspace. */
+#define NBG_DECL_FILL_COLS(T, SFX)                                                                   \
+  NBG_API int nbg_ffill_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner, \
+                                   long long limit, void* stream);                                   \
+  NBG_API int nbg_bfill_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner, \
+                                   long long limit, void* stream);
+NBG_DECL_FILL_COLS(double, f64)
+NBG_DECL_FILL_COLS(float, f32)
+NBG_DECL_FILL_COLS(int, i32)
+NBG_DECL_FILL_COLS(long long, i64)
 
 /* Allocation-free forward fill (float64).  No counterpart in numbagg: it exists for
  * callers that may not allocate device memory -- a host application that owns all GPU

@@ -83,6 +83,30 @@ def rows_last(t: torch.Tensor, axis: int) -> tuple[torch.Tensor, tuple[int, ...]
     return flat, shape
 
 
+# fewest columns for the one-thread-per-column kernels: below this a non-last axis is
+# moved last and copied instead (too few threads would keep the GPU idle)
+MIN_COLUMNS = 2048
+
+
+def column_layout(t: torch.Tensor, axis: int) -> tuple[int, int, int] | None:
+    """(outer, n, inner) when `t` is C-contiguous and `axis` is not its last axis: the
+    array is then `outer` blocks of n x `inner` values, and a kernel with one thread per
+    column scans it along `axis` in place, with no copy (numbagg's gufuncs take such
+    strided core axes directly, numbagg/decorators.py:340-341).  None when that does
+    not apply or the columns are too few to fill the GPU."""
+    if t.ndim < 2 or axis == t.ndim - 1 or not t.is_contiguous():
+        return None
+    outer = 1
+    for d in t.shape[:axis]:
+        outer *= int(d)
+    inner = 1
+    for d in t.shape[axis + 1 :]:
+        inner *= int(d)
+    if outer * inner < MIN_COLUMNS:
+        return None
+    return outer, int(t.shape[axis]), inner
+
+
 def restore_axis(flat: torch.Tensor, shape: tuple[int, ...], axis: int) -> torch.Tensor:
     return torch.movedim(flat.reshape(shape), -1, axis)
 

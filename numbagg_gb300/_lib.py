@@ -106,6 +106,13 @@ def _declare(lib: ctypes.CDLL) -> None:
     for dt in ("f64", "f32", "i32", "i64"):
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+            sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp)
+    # the exponentially weighted family along a non-last axis (one thread per column)
+    for sfx in ("f64", "f32", "f64_fp32c"):
+        for f in ("move_exp_nancount", "move_exp_nanmean", "move_exp_nansum", "move_exp_nanvar", "move_exp_nanstd"):
+            sig(f"nbg_{f}_cols_{sfx}", c_i, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_ll, c_vp)
+        for f in ("move_exp_nancov", "move_exp_nancorr"):
+            sig(f"nbg_{f}_cols_{sfx}", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_ll, c_vp)
     # static aggregations over the last axis
     sig("nbg_aggregate_workspace_bytes", c_sz, c_ll, c_ll)
     for dt in ("f64", "f32", "i32", "i64"):

@@ -182,6 +182,34 @@ __global__ void fill_int_kernel(const T* __restrict__ a, T* __restrict__ out, lo
     out[i] = static_cast<T>(static_cast<double>(a[i]));
 }
 
+// Along a non-last axis of a C-contiguous array (`outer` blocks of n x `inner` values,
+// position p of column i of block o at (o n + p) inner + i): one thread per column
+// carries the last valid position and value down it, so consecutive threads touch
+// consecutive addresses and nothing is copied.  Bit patterns only, as above.
+template <typename T, bool REVERSE>
+__global__ void __launch_bounds__(256) fill_cols_kernel(const T* __restrict__ a, T* __restrict__ out,
+                                                        long long outer, long long n, long long inner,
+                                                        long long limit) {
+  typedef typename BitsOf<T>::type B;
+  const B nan = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  const long long col = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (col >= outer * inner) return;
+  const long long o = col / inner, i = col - o * inner;
+  const B* src = as_bits(a) + o * n * inner + i;
+  B* dst = as_bits(out) + o * n * inner + i;
+  long long last = -1;
+  B lv = B(0);
+  for (long long q = 0; q < n; ++q) {
+    const long long p = REVERSE ? n - 1 - q : q;
+    const B v = src[p * inner];
+    if (!nan_bits(v)) {
+      last = q;
+      lv = v;
+    }
+    dst[p * inner] = (last >= 0 && q - last <= limit) ? lv : nan;
+  }
+}
+
 }  // namespace fill
 }  // namespace nbg
 
@@ -190,6 +218,19 @@ using namespace nbg::fill;
 
 namespace {
 constexpr int kFillK = 16;
+
+template <typename T>
+struct IsFloatT {
+  static constexpr bool value = false;
+};
+template <>
+struct IsFloatT<double> {
+  static constexpr bool value = true;
+};
+template <>
+struct IsFloatT<float> {
+  static constexpr bool value = true;
+};
 
 long long fill_tiles_per_row(long long n) {
   const long long tile = static_cast<long long>(NT) * kFillK;
@@ -232,6 +273,22 @@ int launch_fill_int(const T* a, T* out, long long rows, long long n, long long l
   note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
+template <typename T, bool REVERSE>
+int launch_fill_cols(const T* a, T* out, long long outer, long long n, long long inner, long long limit,
+                     cudaStream_t stream) {
+  if (outer < 0 || n < 0 || inner < 0 || limit < 0) return kInvalidArgument;
+  const long long cols = outer * inner;
+  if (cols == 0 || n == 0) return kOk;
+  if (!a || !out) return kInvalidArgument;
+  const long long blocks = (cols + 255) / 256;
+  if (blocks > 0x7fffffffLL) return kUnsupported;
+  if (IsFloatT<T>::value)
+    fill_cols_kernel<T, REVERSE><<<static_cast<int>(blocks), 256, 0, stream>>>(a, out, outer, n, inner, limit);
+  else
+    fill_int_kernel<T><<<static_cast<int>(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, stream>>>(a, out, cols * n);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
 }  // namespace
 
 extern "C" {
@@ -267,6 +324,21 @@ NBG_FILL_F(double, f64)
 NBG_FILL_F(float, f32)
 NBG_FILL_I(int, i32)
 NBG_FILL_I(long long, i64)
+// Along a non-last axis (fill_cols_kernel).  Integer arrays have no NaN: a copy, as
+// above.
+#define NBG_FILL_COLS(T, SFX)                                                                      \
+  int nbg_ffill_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner,        \
+                           long long limit, void* stream) {                                         \
+    return launch_fill_cols<T, false>(a, out, outer, n, inner, limit, static_cast<cudaStream_t>(stream)); \
+  }                                                                                                 \
+  int nbg_bfill_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner,        \
+                           long long limit, void* stream) {                                         \
+    return launch_fill_cols<T, true>(a, out, outer, n, inner, limit, static_cast<cudaStream_t>(stream)); \
+  }
+NBG_FILL_COLS(double, f64)
+NBG_FILL_COLS(float, f32)
+NBG_FILL_COLS(int, i32)
+NBG_FILL_COLS(long long, i64)
 
 }  // extern "C"
 

@@ -538,12 +538,32 @@ __global__ void exp_pivot_kernel(const T* __restrict__ a, const T* __restrict__ 
 // positions: each thread folds its 8 positions from zero (one multiply-add per state
 // and position); a warp scan with the multipliers d^(8 * 2^i) and a fold over the
 // four warps give every thread the tile-relative state before its run and the tile's
-// aggregate (d^1024, B); the aggregate is published at once and the state entering
-// the tile arrives through decoupled look-back over earlier tiles of the row; each
-// thread then starts from (carry * d^(8 t) + its prefix) and replays its positions,
-// finalising each.  The input is read once, and the divisions of the finalisation
+// aggregate (d^1024, B); the state entering the tile is the inclusive prefix that the
+// row's previous tile published (tiles are claimed row-interleaved, so with many rows
+// it is usually there already), and the tile publishes its own; each thread then
+// starts from (carry * d^(8 t) + its prefix) and replays its positions with the
+// reference's update, finalising each.  The input is read once, and the divisions of the finalisation
 // are float32 reciprocals corrected by one float64 step (about 2^-46 relative) in
 // the float64 arithmetic.  Deterministic: every fold has a fixed order.
+
+// float64 <-> float32 conversions for the seeds of the divisions below, built from the
+// bit patterns on the integer pipes (the FP64 pipe, which bounds these kernels, would
+// otherwise execute the conversions).  Valid for exponents within 120 of 0 (callers
+// check): the float32 keeps the top 23 fraction bits (truncated), the float64 is exact.
+NBG_DEVICE float f32_of(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+  const unsigned e = static_cast<unsigned>((b >> 52) & 0x7ff) - 1023u + 127u;
+  return __uint_as_float(sign | (e << 23) | static_cast<unsigned>((b >> 29) & 0x7fffffu));
+}
+NBG_DEVICE double f64_of(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned long long sign = static_cast<unsigned long long>(b >> 31) << 63;
+  const unsigned long long e = static_cast<unsigned long long>(((b >> 23) & 0xff) - 127u + 1023u);
+  return __longlong_as_double(static_cast<long long>(sign | (e << 52) | (static_cast<unsigned long long>(b & 0x7fffffu) << 29)));
+}
+// about 1 / b to float32 precision (2^-22 or so), b's exponent within 120 of 0
+NBG_DEVICE double rcp_seed(double b) { return f64_of(__frcp_rn(f32_of(b))); }
 
 // a / b within about 2^-46: a float32 reciprocal of b seeds one float64 correction;
 // exponents far from 1, zeros, infinities and NaN take the IEEE division
@@ -551,7 +571,7 @@ NBG_DEVICE double fdiv(double a, double b) {
   const unsigned eb = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(b)) >> 52) & 0x7ffu;
   const unsigned ea = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7ffu;
   if (eb < 1023 - 120 || eb > 1023 + 120 || ea == 0x7ffu) return a / b;
-  const double r = static_cast<double>(__frcp_rn(__double2float_rn(b)));
+  const double r = rcp_seed(b);
   const double q0 = a * r;
   return fma(fma(-q0, b, a), r, q0);
 }
@@ -560,9 +580,9 @@ NBG_DEVICE double fdiv(double a, double b) {
 NBG_DEVICE double fsqrt(double v) {
   const unsigned ev = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(v)) >> 52);
   if (ev < 1023 - 120 || ev > 1023 + 120) return sqrt(v);  // also every negative v (sign bit set)
-  const float rf = rsqrtf(__double2float_rn(v));
-  const double y0 = v * static_cast<double>(rf);
-  return fma(fma(-y0, y0, v), static_cast<double>(0.5f * rf), y0);
+  const float rf = rsqrtf(f32_of(v));
+  const double y0 = v * f64_of(rf);
+  return fma(fma(-y0, y0, v), f64_of(0.5f * rf), y0);
 }
 
 // a / b nearly correctly rounded (Markstein's sequence: the float32 reciprocal refined
@@ -573,10 +593,23 @@ NBG_DEVICE double mdiv(double a, double b) {
   const unsigned eb = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(b)) >> 52) & 0x7ffu;
   const unsigned ea = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7ffu;
   if (eb < 1023 - 120 || eb > 1023 + 120 || ea == 0x7ffu) return a / b;
-  double r = static_cast<double>(__frcp_rn(__double2float_rn(b)));
+  double r = rcp_seed(b);
   r = fma(fma(-b, r, 1.0), r, r);
   const double q0 = a * r;
   return fma(fma(-q0, b, a), r, q0);
+}
+
+// x >= y for float64 values on the integer pipes (false if either is NaN): the
+// comparisons of the finalisation, which the FP64 pipe would otherwise execute
+NBG_DEVICE bool ge_f64(double x, double y) {
+  const unsigned long long bx = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long by = static_cast<unsigned long long>(__double_as_longlong(y));
+  if (nan_bits(bx) || nan_bits(by)) return false;
+  return order_key_ieee(x) >= order_key_ieee(y);
+}
+NBG_DEVICE bool gt0_f64(double x) {  // x > 0 (false for NaN and both zeros)
+  const long long b = __double_as_longlong(x);
+  return b > 0 && !nan_bits(static_cast<unsigned long long>(b));
 }
 
 // The reference's formulas (finalize(F64, ...)), in the reference's order, with the
@@ -584,14 +617,14 @@ NBG_DEVICE double mdiv(double a, double b) {
 template <int OP>
 NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
-  if (OP == kCount) return s[1] >= min_weight ? s[0] : nan;
-  if (OP == kMean) return s[2] >= min_weight ? fdiv(s[0], s[1]) : nan;
-  if (OP == kSum) return (s[1] >= min_weight && seen) ? s[0] : nan;
+  if (OP == kCount) return ge_f64(s[1], min_weight) ? s[0] : nan;
+  if (OP == kMean) return ge_f64(s[2], min_weight) ? fdiv(s[0], s[1]) : nan;
+  if (OP == kSum) return (ge_f64(s[1], min_weight) && seen) ? s[0] : nan;
   if (OP == kVar || OP == kStd) {  // numbagg/moving_exp.py:142-156
     const double m = mdiv(s[1], s[2]);
     const double var_biased = mdiv(s[0], s[2]) - m * m;
     const double bias = 1.0 - mdiv(s[3], s[2] * s[2]);
-    if (s[4] >= min_weight && bias > 0) {
+    if (ge_f64(s[4], min_weight) && gt0_f64(bias)) {
       const double v = fdiv(var_biased, bias);
       return OP == kStd ? fsqrt(v) : v;
     }
@@ -600,16 +633,16 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   if (OP == kCov) {  // numbagg/moving_exp.py:265-273
     const double cov_biased = fdiv(s[2] - mdiv(s[0] * s[1], s[3]), s[3]);
     const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
-    return (s[5] >= min_weight && bias > 0) ? fdiv(cov_biased, bias) : nan;
+    return (ge_f64(s[5], min_weight) && gt0_f64(bias)) ? fdiv(cov_biased, bias) : nan;
   }
   // kCorr, numbagg/moving_exp.py:318-335
   const double cov = s[2] - mdiv(s[0] * s[1], s[3]);
   const double var1 = s[6] - mdiv(s[0] * s[0], s[3]);
   const double var2 = s[7] - mdiv(s[1] * s[1], s[3]);
   const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
-  if (s[5] >= min_weight && bias > 0) {
+  if (ge_f64(s[5], min_weight) && gt0_f64(bias)) {
     const double den = fsqrt(var1 * var2);
-    return den > 0 ? fdiv(cov, den) : nan;
+    return gt0_f64(den) ? fdiv(cov, den) : nan;
   }
   return nan;
 }
@@ -627,14 +660,20 @@ NBG_DEVICE dfl::df df_div_fast(dfl::df x, dfl::df y) {
   const df e = df_sub(x, df_mul_f(y, q1));
   return fast_two_sum(q1, __fmul_rn(e.hi, r));
 }
+// hi + lo in float64 (two conversions and an add on the FP64 pipe, which this form
+// leaves idle) instead of the integer renormalisation of df_to_f64
+NBG_DEVICE double df_out(dfl::df x) {
+  if (!isfinite(x.hi)) return static_cast<double>(x.hi);
+  return static_cast<double>(x.hi) + static_cast<double>(x.lo);
+}
 template <int OP>
 NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
   using namespace dfl;
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   const df one{1.0f, 0.0f};
-  if (OP == kCount) return df_ge_df(s[1], mw) ? df_to_f64(s[0]) : nan;
-  if (OP == kMean) return df_ge_df(s[2], mw) ? df_to_f64(df_div_fast(s[0], s[1])) : nan;
-  if (OP == kSum) return (df_ge_df(s[1], mw) && seen) ? df_to_f64(s[0]) : nan;
+  if (OP == kCount) return df_ge_df(s[1], mw) ? df_out(s[0]) : nan;
+  if (OP == kMean) return df_ge_df(s[2], mw) ? df_out(df_div_fast(s[0], s[1])) : nan;
+  if (OP == kSum) return (df_ge_df(s[1], mw) && seen) ? df_out(s[0]) : nan;
   if (OP == kVar || OP == kStd) {
     const df rw = df_div_fast(one, s[2]);
     const df m = df_mul(s[1], rw);
@@ -642,9 +681,9 @@ NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
     const df bias = df_sub(one, df_mul(s[3], df_mul(rw, rw)));
     if (df_ge_df(s[4], mw) && df_pos(bias)) {
       const df v = df_div_fast(var_biased, bias);
-      if (OP == kVar) return df_to_f64(v);
+      if (OP == kVar) return df_out(v);
       if (v.hi < 0.0f) return nan;
-      return v.hi == 0.0f ? 0.0 : df_to_f64(df_sqrt(v));
+      return v.hi == 0.0f ? 0.0 : df_out(df_sqrt(v));
     }
     return nan;
   }
@@ -652,7 +691,7 @@ NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
   const df bias = df_sub(one, df_mul(s[4], df_mul(rw, rw)));
   if (OP == kCov) {
     const df cov_biased = df_mul(df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw)), rw);
-    return (df_ge_df(s[5], mw) && df_pos(bias)) ? df_to_f64(df_div_fast(cov_biased, bias)) : nan;
+    return (df_ge_df(s[5], mw) && df_pos(bias)) ? df_out(df_div_fast(cov_biased, bias)) : nan;
   }
   const df cov = df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw));
   const df var1 = df_sub(s[6], df_mul(df_mul(s[0], s[0]), rw));
@@ -660,7 +699,7 @@ NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
   if (df_ge_df(s[5], mw) && df_pos(bias)) {
     const df vv = df_mul(var1, var2);
     if (!df_pos(vv)) return nan;
-    return df_to_f64(df_div_fast(cov, df_sqrt(vv)));
+    return df_out(df_div_fast(cov, df_sqrt(vv)));
   }
   return nan;
 }
@@ -673,13 +712,6 @@ template <int OP>
 NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double, dfl::df mw) {
   return finalize_dfast<OP>(s, seen, mw);
 }
-
-template <int OP, typename N>
-struct MapOp {
-  using M = Map<Traits<OP>::NS, N>;
-  NBG_DEVICE M identity() const { return identity_map<OP, N>(); }
-  NBG_DEVICE M combine(const M& earlier, const M& later) const { return compose<OP, N>(earlier, later); }
-};
 
 template <typename N>
 NBG_DEVICE typename N::T pow_n(typename N::T x, int e) {  // x^e for e >= 0, by squaring
@@ -847,17 +879,19 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
           agg.seen |= wseen[u];
         }
       }
+      // chained look-back: wait for the inclusive prefix of the row's previous tile
+      // (claimed `rows` claims earlier, so usually finished) and publish this tile's;
+      // composing in that fixed order keeps the result independent of timing
       M excl = identity_map<OP, N>();
-      if (chunk == 0) {
-        if (lane == 0 && tiles_per_row > 1) publish(ws, tile, epoch, kStatePrefix, agg);
-      } else {
-        if (lane == 0) publish(ws, tile, epoch, kStateAggregate, agg);
-        __syncwarp();
-        bool ok;
-        excl = warp_lookback<M>(ws, tile, chunk, rows, epoch, MapOp<OP, N>(), ok);
-        if (lane == 0) publish(ws, tile, epoch, kStatePrefix, compose<OP, N>(excl, agg));
+      if (lane == 0) {
+        if (chunk > 0) {
+          const long long pred = tile - rows;
+          if (wait_status(ws, pred, epoch) == kStatePrefix) excl = read_payload<M>(ws, pred, kStatePrefix);
+          else record_error(ws.hdr, kLookbackTimeout, static_cast<unsigned>(tile));
+        }
+        if (chunk + 1 < tiles_per_row) publish(ws, tile, epoch, kStatePrefix, compose<OP, N>(excl, agg));
+        carry_smem = excl;
       }
-      if (lane == 0) carry_smem = excl;
     }
     __syncthreads();
     // ---- replay from the state entering this thread's run ----
@@ -873,12 +907,18 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
       load(k, x, y, valid);
       V bj[NS];
       contributions<OP, N>(x, y, al, bj);
+      // the variance family takes the reference's update (a rounded multiply, then a
+      // rounded add): its bias 1 - sw2 / sw^2 can cancel to a few ulps and amplify any
+      // other rounding; count, mean and sum use one multiply-add
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
-        // a missing value contributes zero: one multiply-add either way (s * f + 0
-        // rounds like the product alone)
-        if (!valid) bj[j] = N::zero();
-        s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
+        if (Traits<OP>::PIVOT) {
+          s[j] = N::mul(s[j], (j == W2) ? dd : d);
+          if (valid) s[j] = N::add(s[j], bj[j]);
+        } else {
+          if (!valid) bj[j] = N::zero();
+          s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
+        }
       }
       seen |= valid ? 1 : 0;
       res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight, mw_n));
@@ -900,6 +940,83 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
   if (tid == 0) finish_cta(ws.hdr);
 }
 
+// ---------------------------------------------------------------------------------
+// Along a non-last axis: one thread per column
+// ---------------------------------------------------------------------------------
+// A C-contiguous array scanned along axis k is a batch of `outer` blocks of n x `inner`
+// values: position p of column i of block o sits at (o n + p) inner + i.  Each thread
+// owns one column and runs the reference's loop down it (a rounded multiply, then a
+// rounded add, and the reference's finalisation), so consecutive threads read
+// consecutive addresses and nothing is copied or transposed.  With the float64
+// arithmetic this is numbagg's own sequence of operations.  alpha_mode 0: scalar;
+// 1: n values along the axis; 2: one per element, laid out like `a`.
+template <int OP, typename T, typename N>
+__global__ void __launch_bounds__(256) exp_cols_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                       const T* __restrict__ alpha_arr, double alpha_scalar,
+                                                       int alpha_mode, double min_weight, T* __restrict__ out,
+                                                       long long outer, long long n, long long inner) {
+  constexpr int NS = Traits<OP>::NS;
+  constexpr bool TWO = Traits<OP>::TWO;
+  constexpr bool SHIFT = Traits<OP>::PIVOT && N::kDF;
+  typedef typename BitsOf<T>::type B;
+  typedef typename N::T V;
+  const long long col = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (col >= outer * inner) return;
+  const long long o = col / inner, i = col - o * inner;
+  const long long base = o * n * inner + i;
+  const B* ab = as_bits(a) + base;
+  const B* bb = TWO ? as_bits(b) + base : nullptr;
+  const B* alb = alpha_mode == 2 ? as_bits(alpha_arr) + base : as_bits(alpha_arr);
+  const long long astep = alpha_mode == 2 ? inner : 1;
+  // the pivot of the shift-invariant statistics (double-float only): the column's first
+  // finite value, as the row kernels take each row's
+  V px = N::zero(), py = N::zero();
+  if (SHIFT) {
+    for (int w = 0; w < (TWO ? 2 : 1); ++w) {
+      const B* r = w ? bb : ab;
+      for (long long p = 0; p < n; ++p) {
+        const B v = r[p * inner];
+        const bool fin = sizeof(B) == 8 ? ((static_cast<unsigned long long>(v) >> 52 & 0x7ff) != 0x7ff)
+                                        : ((static_cast<unsigned>(v) >> 23 & 0xff) != 0xff);
+        if (fin) {
+          (w ? py : px) = value_as(N(), v);
+          break;
+        }
+      }
+    }
+  }
+  const V al_s = as_num(N(), alpha_scalar);
+  V s[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) s[j] = N::zero();
+  int seen = 0;
+  for (long long p = 0; p < n; ++p) {
+    const B xb = ab[p * inner];
+    const B yb = TWO ? bb[p * inner] : xb;
+    const bool valid = !nan_bits(xb) && !(TWO && nan_bits(yb));
+    const V al = alpha_mode == 0 ? al_s : value_as(N(), alb[p * astep]);
+    const V d = N::sub(N::one(), al);
+    const V dd = N::mul(d, d);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) s[j] = N::mul(s[j], (j == Traits<OP>::W2) ? dd : d);
+    if (valid) {
+      V x = value_as(N(), xb), y = TWO ? value_as(N(), yb) : x;
+      if (SHIFT) {
+        x = N::sub(x, px);
+        if (TWO) y = N::sub(y, py);
+      }
+      V bj[NS];
+      contributions<OP, N>(x, y, al, bj);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) s[j] = N::add(s[j], bj[j]);
+      seen = 1;
+    }
+    const T r = static_cast<T>(finalize<OP>(N(), s, seen, min_weight));
+    as_bits(out)[base + p * inner] = sizeof(T) == 8 ? static_cast<B>(__double_as_longlong(static_cast<double>(r)))
+                                                   : static_cast<B>(__float_as_uint(static_cast<float>(r)));
+  }
+}
+
 }  // namespace mexp
 }  // namespace nbg
 
@@ -909,6 +1026,7 @@ using namespace nbg::mexp;
 namespace {
 
 long long exp_tiles_per_row(long long n) { return n <= 0 ? 0 : (n + TILE - 1) / TILE; }
+constexpr long long kScanMinRows = 32;
 
 // maps and carries for `tiles` tiles (or the look-back workspace of the one-pass scan,
 // whichever is larger), pivots and the ragged plan for `rows` series
@@ -963,7 +1081,9 @@ int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int 
   // an upper bound on the tiles: each series adds at most one partial tile
   const long long tiles = offsets ? total / TILE + rows : rows * exp_tiles_per_row(n);
   if (!ws || ws_bytes < exp_scratch_for(rows, tiles)) return kWorkspaceTooSmall;
-  if (alpha_mode == 0 && !offsets)
+  // the one-pass scan chains tiles row by row: with few rows the chain would serialise,
+  // so those keep the three-phase scan
+  if (alpha_mode == 0 && !offsets && rows >= kScanMinRows)
     return launch_exp_scan<OP, T, N>(a, b, alpha_scalar, min_weight, out, rows, n, ws, s);
   using M = Map<Traits<OP>::NS, N>;
   static_assert(sizeof(M) <= sizeof(Map<Traits<kCorr>::NS, F64>), "8-byte numbers");
@@ -991,6 +1111,20 @@ int launch_exp(const T* a, const T* b, const T* alpha, double alpha_scalar, int 
   exp_tile_kernel<OP, T, N, 2><<<grid, NT, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, lay, maps,
                                                    carries, pivots);
   note_launches(launches);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
+template <int OP, typename T, typename N>
+int launch_exp_cols(const T* a, const T* b, const T* alpha, double alpha_scalar, int alpha_mode, double min_weight,
+                    T* out, long long outer, long long n, long long inner, cudaStream_t s) {
+  if (outer < 0 || n < 0 || inner < 0 || alpha_mode < 0 || alpha_mode > 2) return kInvalidArgument;
+  if (outer == 0 || n == 0 || inner == 0) return kOk;
+  if (!a || !out || (Traits<OP>::TWO && !b) || (alpha_mode > 0 && !alpha)) return kInvalidArgument;
+  const long long cols = outer * inner;
+  const long long blocks = (cols + 255) / 256;
+  if (blocks > 0x7fffffffLL) return kUnsupported;
+  exp_cols_kernel<OP, T, N><<<static_cast<int>(blocks), 256, 0, s>>>(a, b, alpha, alpha_scalar, alpha_mode,
+                                                                      min_weight, out, outer, n, inner);
+  note_launches(1);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
 }  // namespace
@@ -1045,6 +1179,34 @@ NBG_EXP1(move_exp_nanvar, kVar, double, f64_fp32c, DF)
 NBG_EXP1(move_exp_nanstd, kStd, double, f64_fp32c, DF)
 NBG_EXP2(move_exp_nancov, kCov, double, f64_fp32c, DF)
 NBG_EXP2(move_exp_nancorr, kCorr, double, f64_fp32c, DF)
+
+// Along a non-last axis of a C-contiguous array: `outer` blocks of n x `inner` values,
+// scanned along n, one thread per column (exp_cols_kernel).
+#define NBG_EXP1_COLS(NAME, OPC, T, SFX, N)                                                          \
+  int nbg_##NAME##_cols_##SFX(const T* a, const T* alpha, double alpha_scalar, int alpha_mode,        \
+                              double min_weight, T* out, long long outer, long long n, long long inner, \
+                              void* stream) {                                                        \
+    return launch_exp_cols<OPC, T, N>(a, nullptr, alpha, alpha_scalar, alpha_mode, min_weight, out,  \
+                                      outer, n, inner, static_cast<cudaStream_t>(stream));           \
+  }
+#define NBG_EXP2_COLS(NAME, OPC, T, SFX, N)                                                          \
+  int nbg_##NAME##_cols_##SFX(const T* a, const T* b, const T* alpha, double alpha_scalar,            \
+                              int alpha_mode, double min_weight, T* out, long long outer, long long n, \
+                              long long inner, void* stream) {                                       \
+    return launch_exp_cols<OPC, T, N>(a, b, alpha, alpha_scalar, alpha_mode, min_weight, out, outer, n, \
+                                      inner, static_cast<cudaStream_t>(stream));                     \
+  }
+#define NBG_EXP_COLS_ALL(T, SFX, NP)                                  \
+  NBG_EXP1_COLS(move_exp_nancount, kCount, T, SFX, NP)               \
+  NBG_EXP1_COLS(move_exp_nanmean, kMean, T, SFX, NP)                 \
+  NBG_EXP1_COLS(move_exp_nansum, kSum, T, SFX, NP)                   \
+  NBG_EXP1_COLS(move_exp_nanvar, kVar, T, SFX, NP)                   \
+  NBG_EXP1_COLS(move_exp_nanstd, kStd, T, SFX, NP)                   \
+  NBG_EXP2_COLS(move_exp_nancov, kCov, T, SFX, NP)                   \
+  NBG_EXP2_COLS(move_exp_nancorr, kCorr, T, SFX, NP)
+NBG_EXP_COLS_ALL(double, f64, F64)
+NBG_EXP_COLS_ALL(float, f32, F64)
+NBG_EXP_COLS_ALL(double, f64_fp32c, DF)
 
 // Ragged series: series s is values[offsets[s] : offsets[s + 1]] (nseries + 1 offsets on
 // the device, `total` = offsets[nseries]); a scalar alpha (alpha_mode 0) or one per

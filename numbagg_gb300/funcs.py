@@ -55,7 +55,16 @@ def _fill(name: str, arr, limit, axis):
         work = torch.int64
     else:
         work = orig
-    flat, shape = _host.rows_last(a.to(work), axis)
+    aw = a.to(work)
+    cols = _host.column_layout(aw, axis)
+    if cols is not None:  # a non-last axis of a contiguous array: filled in place, no copy
+        outer, n, inner = cols
+        out = torch.empty_like(aw)
+        if out.numel():
+            fn = getattr(_lib.lib(), f"nbg_{name}_cols_{_host.ALL_SFX[work]}")
+            _lib.check(fn(aw.data_ptr(), out.data_ptr(), outer, n, inner, limit, _host.stream(a.device)), name)
+        return restore(out.to(orig) if work != orig else out)
+    flat, shape = _host.rows_last(aw, axis)
     rows, n = flat.shape
     out = torch.empty((rows, n), dtype=work, device=a.device)
     if out.numel():

@@ -73,13 +73,17 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis, precision="f64"):
     dtype = loop_dtype(tensors, alpha, min_weight)
     if len(tensors) > 1:
         tensors = list(torch.broadcast_tensors(*tensors))
+    np_dtype = np.float64 if dtype == torch.float64 else np.float32
+    cols_out = _move_exp_columns(name, [t.to(dtype) for t in tensors], alpha, min_weight, axis, dtype, np_dtype,
+                                 precision)
+    if cols_out is not None:
+        return restore(cols_out)
     flats = []
     shape = None
     for t in tensors:
         f, shape = _host.rows_last(t.to(dtype), axis)
         flats.append(f)
     rows, n = flats[0].shape
-    np_dtype = np.float64 if dtype == torch.float64 else np.float32
 
     alpha_t = None
     alpha_scalar = 0.0
@@ -122,6 +126,49 @@ def _move_exp(name: str, arrs, alpha, min_weight, axis, precision="f64"):
         ]
         _lib.check(fn(*args), name)
     return restore(_host.restore_axis(out, shape, axis))
+
+
+def _move_exp_columns(name, tensors, alpha, min_weight, axis, dtype, np_dtype, precision):
+    """A non-last axis of contiguous arrays: one thread per column runs numbagg's loop
+    down it in place (no copy).  None when the layout does not apply."""
+    cols = _host.column_layout(tensors[0], axis)
+    if cols is None or any(t.shape != tensors[0].shape or not t.is_contiguous() for t in tensors):
+        return None
+    outer, n, inner = cols
+    alpha_t, alpha_scalar = None, 0.0
+    if isinstance(alpha, (np.ndarray, torch.Tensor)) and np.ndim(alpha) > 0:
+        at, _ = _host.to_device(alpha)
+        at = at.to(device=tensors[0].device, dtype=dtype)
+        if at.ndim == 1:
+            if at.shape[0] != n:
+                raise ValueError(f"alpha has length {at.shape[0]}, expected {n} (the length of axis {axis})")
+            alpha_t, mode = at.contiguous(), 1
+        elif tuple(at.shape) == tuple(tensors[0].shape):
+            alpha_t, mode = at.contiguous(), 2
+        else:
+            return None  # a broadcast alpha: the rows path handles it
+    else:
+        alpha_scalar = float(np_dtype(np.asarray(alpha).item() if hasattr(alpha, "shape") else alpha))
+        mode = 0
+    out = torch.empty_like(tensors[0])
+    if out.numel():
+        sfx = _host.FLOAT_SFX[dtype]
+        if precision == "fp32c" and dtype == torch.float64:
+            sfx += "_fp32c"
+        fn = getattr(_lib.lib(), f"nbg_{name}_cols_{sfx}")
+        args = [t.data_ptr() for t in tensors] + [
+            None if alpha_t is None else alpha_t.data_ptr(),
+            alpha_scalar,
+            mode,
+            float(np_dtype(min_weight)),
+            out.data_ptr(),
+            outer,
+            n,
+            inner,
+            _host.stream(tensors[0].device),
+        ]
+        _lib.check(fn(*args), name)
+    return out
 
 
 def move_exp_nancount(arr, /, *, alpha, min_weight=0, axis=-1, precision="f64"):

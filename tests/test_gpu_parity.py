@@ -135,6 +135,22 @@ def test_move_exp_vs_oracle(fname, dtype, alpha, min_weight):
     assert r["allowed"] <= 0.001 * r["n"] + 20
 
 
+@pytest.mark.parametrize("fname", MOVE_EXP)
+@pytest.mark.parametrize("alpha,min_weight", [(0.5, 0.0), (0.9, 0.3), (0.01, 0.0)])
+def test_move_exp_one_pass_vs_oracle(fname, alpha, min_weight):
+    # 40 rows: a scalar alpha over this many rows takes the one-pass scan (tiles chained
+    # row by row), fewer rows the three-phase one
+    x = _data((40, 20_000), 16, normal=False)
+    y = _data((40, 20_000), 17, normal=False) if fname in ("move_exp_nancov", "move_exp_nancorr") else None
+    func = getattr(nb, fname)
+    got = func(x, y, alpha=alpha, min_weight=min_weight) if y is not None else func(x, alpha=alpha, min_weight=min_weight)
+    want = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight)
+    ext = oracle.move_exp(fname, x, y, alpha=alpha, min_weight=min_weight, ext=True)
+    allow = exp_degenerate(fname, x, y, alpha, min_weight)
+    r = assert_parity(got, want, ext, exp_scale(fname, x, y, alpha), F64_TOL, allow, fname)
+    assert r["allowed"] <= 0.001 * r["n"] + 50
+
+
 @pytest.mark.parametrize("fname", ["move_exp_nanmean", "move_exp_nanvar", "move_exp_nancorr"])
 def test_move_exp_alpha_forms(fname):
     # numbagg/test/test_moving_exp.py:348-368: scalar, 1-D and N-D alpha agree
@@ -372,20 +388,24 @@ def test_move_matrix_known_answers():
 
 
 @pytest.mark.parametrize("fname", ["move_mean", "move_std", "move_exp_nanvar", "ffill"])
-def test_prefix_causality_bit_exact(fname):
+@pytest.mark.parametrize("rows", [4, 64])
+def test_prefix_causality_bit_exact(fname, rows):
     """A prefix of a longer input gives bit-identical results
-    (numbagg/test/test_property.py:86-150)."""
-    x = torch.randn(4, 3_000_001, dtype=torch.float64, device="cuda")
+    (numbagg/test/test_property.py:86-150); 64 rows take the one-pass EWM scan."""
+    x = torch.randn(rows, 3_000_001 if rows == 4 else 400_001, dtype=torch.float64, device="cuda")
     x[torch.rand_like(x) < 0.05] = float("nan")
     func = getattr(nb, fname)
     kw = {"window": 20} if fname.startswith("move_") and "exp" not in fname else {}
     if "exp" in fname:
         kw = {"alpha": 0.01}
+    cut = 2_000_000 if rows == 4 else 250_000
     full = func(x, **kw)
-    part = func(x[:, :2_000_000].contiguous(), **kw)
-    assert torch.equal(torch.isnan(full[:, :2_000_000]), torch.isnan(part))
+    part = func(x[:, :cut].contiguous(), **kw)
+    again = func(x, **kw)
+    assert torch.equal(torch.isnan(full[:, :cut]), torch.isnan(part))
     m = ~torch.isnan(part)
-    assert torch.equal(full[:, :2_000_000][m], part[m])
+    assert torch.equal(full[:, :cut][m], part[m])
+    assert torch.equal(torch.nan_to_num(full, nan=7.0), torch.nan_to_num(again, nan=7.0))  # run to run
 
 
 @pytest.fixture
