@@ -1148,8 +1148,11 @@ __global__ void big_mom_finish_kernel(const double* __restrict__ acc1, const dou
     if (F == kCount) res = static_cast<O>(cnt);
     else if (F == kSum) res = static_cast<O>(s1);
     else if (F == kSumSq) res = static_cast<O>(s2);
-    else if (F == kMean) res = static_cast<O>(cnt == 0 ? nan : div_by_count(s1, cnt, rcp));
-    else {
+    else if (F == kMean) {
+      // s1 / c as the product by the tabled reciprocal (within an ulp of the quotient)
+      const bool tab = cnt <= kRcpN && isfinite(s1);
+      res = static_cast<O>(cnt == 0 ? nan : (tab ? s1 * __ldg(rcp + cnt) : s1 / static_cast<double>(cnt)));
+    } else {
       // (s2 - s1^2 / c) / (c - ddof), numbagg/grouped.py:170-176, with the divisions as
       // products by the tabled reciprocals (within an ulp of each quotient; the
       // subtraction's cancellation is the reference's own)

@@ -575,16 +575,6 @@ NBG_DEVICE double fdiv(double a, double b) {
   const double q0 = a * r;
   return fma(fma(-q0, b, a), r, q0);
 }
-// sqrt(v) within about 2^-46 the same way (a float32 reciprocal square root, one
-// float64 Newton step); v <= 0, infinities, NaN and extreme exponents take sqrt
-NBG_DEVICE double fsqrt(double v) {
-  const unsigned ev = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(v)) >> 52);
-  if (ev < 1023 - 120 || ev > 1023 + 120) return sqrt(v);  // also every negative v (sign bit set)
-  const float rf = rsqrtf(f32_of(v));
-  const double y0 = v * f64_of(rf);
-  return fma(fma(-y0, y0, v), f64_of(0.5f * rf), y0);
-}
-
 // a / b nearly correctly rounded (Markstein's sequence: the float32 reciprocal refined
 // once, then the quotient corrected once; P. Markstein, IBM J. Res. Dev. 34(1), 1990):
 // for the quotients that feed a cancellation (the bias 1 - sw2 / sw^2 and the biased
@@ -620,20 +610,23 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   if (OP == kCount) return ge_f64(s[1], min_weight) ? s[0] : nan;
   if (OP == kMean) return ge_f64(s[2], min_weight) ? fdiv(s[0], s[1]) : nan;
   if (OP == kSum) return (ge_f64(s[1], min_weight) && seen) ? s[0] : nan;
+  // the variance family: the bias 1 - sw2 / sw^2 can cancel to a few ulps, so the
+  // statistic can be many times its natural scale and every quotient and root here is
+  // taken nearly correctly rounded (mdiv, sqrt)
   if (OP == kVar || OP == kStd) {  // numbagg/moving_exp.py:142-156
     const double m = mdiv(s[1], s[2]);
     const double var_biased = mdiv(s[0], s[2]) - m * m;
     const double bias = 1.0 - mdiv(s[3], s[2] * s[2]);
     if (ge_f64(s[4], min_weight) && gt0_f64(bias)) {
-      const double v = fdiv(var_biased, bias);
-      return OP == kStd ? fsqrt(v) : v;
+      const double v = mdiv(var_biased, bias);
+      return OP == kStd ? sqrt(v) : v;
     }
     return nan;
   }
   if (OP == kCov) {  // numbagg/moving_exp.py:265-273
-    const double cov_biased = fdiv(s[2] - mdiv(s[0] * s[1], s[3]), s[3]);
+    const double cov_biased = mdiv(s[2] - mdiv(s[0] * s[1], s[3]), s[3]);
     const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
-    return (ge_f64(s[5], min_weight) && gt0_f64(bias)) ? fdiv(cov_biased, bias) : nan;
+    return (ge_f64(s[5], min_weight) && gt0_f64(bias)) ? mdiv(cov_biased, bias) : nan;
   }
   // kCorr, numbagg/moving_exp.py:318-335
   const double cov = s[2] - mdiv(s[0] * s[1], s[3]);
@@ -641,11 +634,12 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   const double var2 = s[7] - mdiv(s[1] * s[1], s[3]);
   const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
   if (ge_f64(s[5], min_weight) && gt0_f64(bias)) {
-    const double den = fsqrt(var1 * var2);
-    return gt0_f64(den) ? fdiv(cov, den) : nan;
+    const double den = sqrt(var1 * var2);
+    return gt0_f64(den) ? mdiv(cov, den) : nan;
   }
   return nan;
 }
+
 // Double-float finalisation of the one-pass scan: min_weight converted once per
 // kernel, comparisons on the (hi, lo) pair, and divisions as one float32 quotient plus
 // one correction (about 2^-44 relative, far inside the compensated form's bound).
