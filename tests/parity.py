@@ -151,7 +151,32 @@ def move_scale(name, a, b, window, axis=-1):
     return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)))
 
 
+def exp_bias(a, b, alpha, axis=-1):
+    """The bias term 1 - sw2 / sw^2 of the variance family (numbagg/moving_exp.py:142-150)
+    over the (pairwise) valid positions: sw = sum of decayed weights, the decayed count
+    move_exp_nancount gives, and sw2 the same with every decay squared (alpha' = 1 -
+    (1 - alpha)^2).  Where it cancels towards 0 the reference's float64 evaluation
+    amplifies every rounding in its running sums by 1 / bias."""
+    v = _valid(a, b).astype(np.float64)
+    ind = np.where(v > 0, 1.0, np.nan)
+    al = alpha if not isinstance(alpha, np.ndarray) else alpha.astype(np.float64)
+    al2 = 1.0 - (1.0 - np.asarray(al, dtype=np.float64)) ** 2
+    if not isinstance(alpha, np.ndarray):
+        al2 = float(al2)
+    sw = oracle.move_exp("move_exp_nancount", ind, alpha=al, axis=axis, ext=True)
+    sw2 = oracle.move_exp("move_exp_nancount", ind, alpha=al2, axis=axis, ext=True)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        bias = 1.0 - sw2 / (sw * sw)
+    return np.where(np.isfinite(bias) & (bias > 0), bias, np.nan)
+
+
 def exp_scale(name, a, b, alpha, axis=-1):
+    """Natural magnitude of each statistic's rounding: the weighted mean of |x| or x^2;
+    for the variance family the result is a biased value divided by the bias term (see
+    exp_bias), whose own rounding (~eps absolute) adds |value| * eps / bias, so the scale
+    is (mean(x^2) + |value|) / bias; the correlation's bias cancels
+    (numbagg/moving_exp.py:319), its scale is the conditioning mean(x^2) / (var * bias)
+    of either input's unnormalised weighted variance."""
     a64 = np.asarray(a, dtype=np.float64)
     absa = np.abs(a64)
     if name == "move_exp_nancount":
@@ -162,20 +187,29 @@ def exp_scale(name, a, b, alpha, axis=-1):
     if name == "move_exp_nanmean":
         return oracle.move_exp("move_exp_nanmean", absa, alpha=al, axis=axis)
     sq = oracle.move_exp("move_exp_nanmean", absa * absa, alpha=al, axis=axis)
-    if name == "move_exp_nanvar":
-        return sq
-    if name == "move_exp_nanstd":
-        std = oracle.move_exp("move_exp_nanstd", a64, alpha=al, axis=axis)
+    bias = exp_bias(a, b if name in ("move_exp_nancov", "move_exp_nancorr") else None, alpha, axis)
+    amp = np.where(np.isnan(bias), 1.0, 1.0 / np.fmax(bias, 1e-300))
+    if name in ("move_exp_nanvar", "move_exp_nanstd"):
+        var = np.abs(np.nan_to_num(oracle.move_exp("move_exp_nanvar", a64, alpha=al, axis=axis, ext=True)))
+        svar = (sq + var) * amp
+        if name == "move_exp_nanvar":
+            return svar
+        std = np.sqrt(var)
         with np.errstate(invalid="ignore", divide="ignore"):
-            return np.fmax(np.sqrt(sq), sq / std)
-    b64 = np.asarray(b, dtype=np.float64)
-    absb = np.abs(b64)
+            return np.fmax(np.sqrt(svar), svar / std)
+    # the pair functions see only the positions where both inputs are valid
+    v = _valid(a, b)
+    a64 = np.where(v, a64, np.nan)
+    b64 = np.where(v, np.asarray(b, dtype=np.float64), np.nan)
+    absa, absb = np.abs(a64), np.abs(b64)
+    sq = oracle.move_exp("move_exp_nanmean", absa * absa, alpha=al, axis=axis)
     sqb = oracle.move_exp("move_exp_nanmean", absb * absb, alpha=al, axis=axis)
     if name == "move_exp_nancov":
-        return np.sqrt(sq * sqb)
+        cov = np.abs(np.nan_to_num(oracle.move_exp("move_exp_nancov", a64, b64, alpha=al, axis=axis, ext=True)))
+        return (np.sqrt(sq * sqb) + cov) * amp
     va = oracle.move_exp("move_exp_nanvar", a64, alpha=al, axis=axis)
     vb = oracle.move_exp("move_exp_nanvar", b64, alpha=al, axis=axis)
-    return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)))
+    return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)) * amp)
 
 
 # ---- degenerate positions ---------------------------------------------------------------
