@@ -1078,6 +1078,10 @@ def run_aggregate_suite(args):
         "nanargmax": lambda: nb.nanargmax(values, axis=-1),
         "anynan": lambda: nb.anynan(values, axis=-1),
         "nansum_all_axes": lambda: nb.nansum(values),
+        # the same buffer as (cols, 64) reduced over its first axis: in place through the
+        # stride, no copy
+        "nansum_axis0": lambda: nb.nansum(values.view(args.cols, ROWS), axis=0),
+        "nanvar_axis0": lambda: nb.nanvar(values.view(args.cols, ROWS), axis=0),
     }
     peak, peak_kind = measured_peak()
     stream = torch.cuda.current_stream(device)
@@ -1100,7 +1104,8 @@ def run_aggregate_suite(args):
     line = {
         "suite": "aggregate",
         "metric": "HBM GB/s of the static aggregations (8 bytes read per element)",
-        "config": {"values": f"float64 {ROWS} x {args.cols}, N(0,1), {NAN_P:.0%} NaN", "axis": -1},
+        "config": {"values": f"float64 {ROWS} x {args.cols}, N(0,1), {NAN_P:.0%} NaN",
+                   "axis": "-1; *_axis0: the buffer viewed as cols x 64, axis 0"},
         "peak": peak,
         "peak_kind": peak_kind,
         "per_func": res,

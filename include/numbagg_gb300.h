@@ -97,6 +97,26 @@ NBG_DECL_MOVE1(move_var, double, f64_fp32c)
 NBG_DECL_MOVE1(move_std, double, f64_fp32c)
 NBG_DECL_MOVE2(move_cov, double, f64_fp32c)
 NBG_DECL_MOVE2(move_corr, double, f64_fp32c)
+/* Along a non-last axis of a C-contiguous array (the strided core axis numbagg's
+ * gufuncs accept, numbagg/decorators.py:340-341): `outer` blocks of n x `inner`
+ * values, position p of column i of block o at (o * n + p) * inner + i, scanned along
+ * n in place by one thread per column running numbagg's loop (the reference's float64
+ * arithmetic, bit for bit).  No workspace. */
+#define NBG_DECL_MOVE1_COLS(NAME, T, SFX)                                                        \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner, \
+                                      long long window, long long min_count, void* stream);
+#define NBG_DECL_MOVE2_COLS(NAME, T, SFX)                                                        \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, const T* b, T* out, long long outer, long long n,    \
+                                      long long inner, long long window, long long min_count, void* stream);
+#define NBG_DECL_MOVE_COLS_ALL(T, SFX)  \
+  NBG_DECL_MOVE1_COLS(move_sum, T, SFX)  \
+  NBG_DECL_MOVE1_COLS(move_mean, T, SFX) \
+  NBG_DECL_MOVE1_COLS(move_var, T, SFX)  \
+  NBG_DECL_MOVE1_COLS(move_std, T, SFX)  \
+  NBG_DECL_MOVE2_COLS(move_cov, T, SFX)  \
+  NBG_DECL_MOVE2_COLS(move_corr, T, SFX)
+NBG_DECL_MOVE_COLS_ALL(double, f64)
+NBG_DECL_MOVE_COLS_ALL(float, f32)
 
 /* Ragged batches of moving windows (no reference counterpart: numbagg applies its
  * functions array by array; these run many series of uneven length in one call).
@@ -360,7 +380,7 @@ NBG_DECL_PAIR_MATRIX(nancovmatrix, float, f32)
 NBG_DECL_PAIR_MATRIX(nancorrmatrix, double, f64)
 NBG_DECL_PAIR_MATRIX(nancorrmatrix, float, f32)
 
-/* ---- static aggregations over the last axis ----------------------------------------
+/* ---- static aggregations ------------------------------------------------------------
  * Replace numbagg/funcs.py:23-159 (ndaggregate: allnan, anynan, nancount, nansum,
  * nanmean, nanvar, nanstd) and :162-242 (ndreduce: nanargmax, nanargmin, nanmax,
  * nanmin).  a is a C-contiguous (rows, m) view whose last axis holds the reduced axes
@@ -373,13 +393,22 @@ NBG_DECL_PAIR_MATRIX(nancorrmatrix, float, f32)
  *                        integer nansum wraps like the reference's integer loop)
  * nanvar / nanstd take ddof (NaN unless count > ddof and count > 0).  nanmax / nanmin / nanarg*
  * with m == 0 return NBG_INVALID_ARGUMENT (numbagg raises on an empty reduction).
- * ws: nbg_aggregate_workspace_bytes(rows, m) bytes of scratch, no initialisation. */
+ * ws: nbg_aggregate_workspace_bytes(rows, m) bytes of scratch, no initialisation.
+ * The _cols entry points reduce the middle axis of a C-contiguous (outer, m, inner)
+ * array in place (reduced axes that are consecutive and not last, as numbagg's gufuncs
+ * read them through strides): out[o * inner + i] reduces a[(o * m + r) * inner + i]
+ * over r, and nanarg* return r; ws: nbg_aggregate_cols_workspace_bytes(outer, m, inner). */
 NBG_API size_t nbg_aggregate_workspace_bytes(long long rows, long long m);
-#define NBG_DECL_AGG(NAME, T, O, SFX) \
-  NBG_API int nbg_##NAME##_##SFX(const T* a, O* out, long long rows, long long m, void* ws, size_t ws_bytes, void* stream);
+NBG_API size_t nbg_aggregate_cols_workspace_bytes(long long outer, long long m, long long inner);
+#define NBG_DECL_AGG(NAME, T, O, SFX)                                                                      \
+  NBG_API int nbg_##NAME##_##SFX(const T* a, O* out, long long rows, long long m, void* ws, size_t ws_bytes, void* stream); \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, O* out, long long outer, long long m, long long inner, void* ws,     \
+                                      size_t ws_bytes, void* stream);
 #define NBG_DECL_AGG_DDOF(NAME, T, SFX)                                                                      \
   NBG_API int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long m, long long ddof, void* ws, \
-                                 size_t ws_bytes, void* stream);
+                                 size_t ws_bytes, void* stream);                                            \
+  NBG_API int nbg_##NAME##_cols_##SFX(const T* a, T* out, long long outer, long long m, long long inner,    \
+                                      long long ddof, void* ws, size_t ws_bytes, void* stream);
 #define NBG_DECL_AGG_ALL(NAME, O)          \
   NBG_DECL_AGG(NAME, double, O, f64)       \
   NBG_DECL_AGG(NAME, float, O, f32)        \

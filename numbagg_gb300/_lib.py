@@ -107,6 +107,12 @@ def _declare(lib: ctypes.CDLL) -> None:
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
             sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp)
+    # moving windows along a non-last axis (one thread per column)
+    for dt in ("f64", "f32"):
+        for f in ("move_sum", "move_mean", "move_var", "move_std"):
+            sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
+        for f in ("move_cov", "move_corr"):
+            sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
     # the exponentially weighted family along a non-last axis (one thread per column)
     for sfx in ("f64", "f32", "f64_fp32c"):
         for f in ("move_exp_nancount", "move_exp_nanmean", "move_exp_nansum", "move_exp_nanvar", "move_exp_nanstd"):
@@ -122,6 +128,15 @@ def _declare(lib: ctypes.CDLL) -> None:
         sig(f"nbg_nanmean_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
         for f in ("nanvar", "nanstd"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+    # the same over the middle axis of a contiguous (outer, m, inner) array
+    sig("nbg_aggregate_cols_workspace_bytes", c_sz, c_ll, c_ll, c_ll)
+    for dt in ("f64", "f32", "i32", "i64"):
+        for f in ("allnan", "anynan", "nancount", "nansum", "nanmax", "nanmin", "nanargmax", "nanargmin"):
+            sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+    for dt in ("f64", "f32"):
+        sig(f"nbg_nanmean_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
+        for f in ("nanvar", "nanstd"):
+            sig(f"nbg_{f}_cols_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)
     for name in GROUP_FUNC_IDS:
         vdts = ("f64", "f32") if name in ("nanmean", "nanvar", "nanstd") else ("f64", "f32", "i32", "i64")
         for vd in vdts:

@@ -41,6 +41,8 @@ _TORCH_TO_NP = {
     torch.uint8: np.uint8,
     torch.bool: np.bool_,
 }
+# the in-place path for middle axes wants whole warps of consecutive outputs
+_MIN_INNER = 32
 _NP_TO_TORCH = {np.float64: torch.float64, np.float32: torch.float32, np.int64: torch.int64, np.int32: torch.int32}
 
 
@@ -98,7 +100,20 @@ def _aggregate(name: str, arr, axis, *, ddof=None):
     work = _NP_TO_TORCH[loop]
     if a.dtype != work:
         a = a.to(work)
-    flat = torch.movedim(a, axes, tuple(range(len(shape) - len(axes), len(shape)))).contiguous().reshape(rows, m)
+    # reduced axes that are consecutive, in increasing order and not last: reduced in
+    # place through their stride (numbagg's gufuncs read them so), no copy
+    k0 = axes[0] if axes else 0
+    inner = math.prod(shape[axes[-1] + 1 :]) if axes else 1
+    middle = (
+        len(axes) > 0
+        and axes == tuple(range(k0, k0 + len(axes)))
+        and axes[-1] < len(shape) - 1
+        and inner >= _MIN_INNER
+        and a.is_contiguous()
+    )
+    flat = None
+    if not middle:
+        flat = torch.movedim(a, axes, tuple(range(len(shape) - len(axes), len(shape)))).contiguous().reshape(rows, m)
     if name in ("allnan", "anynan"):
         out_dt = torch.bool
     elif name in ("nancount", "nanargmax", "nanargmin"):
@@ -108,9 +123,15 @@ def _aggregate(name: str, arr, axis, *, ddof=None):
     out = torch.empty(rows, dtype=out_dt, device=a.device)
     if rows > 0:
         L = _lib.lib()
-        ws = _lib.workspaces.scratch(L.nbg_aggregate_workspace_bytes(rows, m), a.device)
-        fn = getattr(L, f"nbg_{name}_{_host.ALL_SFX[work]}")
-        args = [flat.data_ptr() if m > 0 else None, out.data_ptr(), rows, m]
+        if middle:
+            outer = rows // inner
+            ws = _lib.workspaces.scratch(L.nbg_aggregate_cols_workspace_bytes(outer, m, inner), a.device)
+            fn = getattr(L, f"nbg_{name}_cols_{_host.ALL_SFX[work]}")
+            args = [a.data_ptr() if m > 0 else None, out.data_ptr(), outer, m, inner]
+        else:
+            ws = _lib.workspaces.scratch(L.nbg_aggregate_workspace_bytes(rows, m), a.device)
+            fn = getattr(L, f"nbg_{name}_{_host.ALL_SFX[work]}")
+            args = [flat.data_ptr() if m > 0 else None, out.data_ptr(), rows, m]
         if ddof is not None:
             args.append(ddof)
         _lib.check(fn(*args, ws.data_ptr(), ws.numel(), _host.stream(a.device)), name)

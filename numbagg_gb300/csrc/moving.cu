@@ -571,6 +571,148 @@ __global__ void move_poison_kernel(T* __restrict__ out, Layout lay, long long wi
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Along a non-last axis: one thread per column
+// ---------------------------------------------------------------------------------
+// A C-contiguous array scanned along axis k is `outer` blocks of n x `inner` values:
+// position p of column i of block o sits at (o n + p) inner + i.  Each thread owns one
+// column and runs numbagg's loop down it with its float64 running sums, operation for
+// operation (rounded multiplies, adds and divisions, never contracted into a multiply-
+// add; float32 values widened to float64 as numba's float64 locals take them), so the
+// results are the reference's bit for bit, infinities included.  Consecutive threads
+// read consecutive addresses at every step, and nothing is copied or transposed.
+NBG_DEVICE double ld_col(const double* p) { return __ldg(p); }
+NBG_DEVICE double ld_col(const float* p) { return static_cast<double>(__ldg(p)); }
+NBG_DEVICE bool isnan_d(double x) { return nan_bits(static_cast<unsigned long long>(__double_as_longlong(x))); }
+
+template <int OP, typename T>
+__global__ void __launch_bounds__(256) move_cols_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                        T* __restrict__ out, long long outer, long long n,
+                                                        long long inner, long long window, long long min_count) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const long long col = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (col >= outer * inner) return;
+  const long long o = col / inner, c = col - o * inner;
+  const long long base = o * n * inner + c;
+  const T* ac = a + base;
+  const T* bc = Traits<OP>::TWO ? b + base : nullptr;
+  T* oc = out + base;
+  if (OP == kSum || OP == kMean) {  // numbagg/moving.py:12-55, :58-99
+    const long long mc = OP == kMean ? (min_count > 1 ? min_count : 1) : min_count;
+    double asum = 0.0;
+    long long count = 0;
+    const long long w0 = window < n ? window : n;
+    for (long long p = 0; p < w0; ++p) {
+      const double ai = ld_col(ac + p * inner);
+      if (!isnan_d(ai)) {
+        asum = __dadd_rn(asum, ai);
+        ++count;
+      }
+      oc[p * inner] = static_cast<T>(count >= mc ? (OP == kMean ? __ddiv_rn(asum, static_cast<double>(count)) : asum) : nan);
+    }
+    for (long long p = window; p < n; ++p) {
+      const double ai = ld_col(ac + p * inner);
+      const double aold = ld_col(ac + (p - window) * inner);
+      if (OP == kMean) {  // removes the old value first
+        if (!isnan_d(aold)) {
+          asum = __dsub_rn(asum, aold);
+          --count;
+        }
+        if (!isnan_d(ai)) {
+          asum = __dadd_rn(asum, ai);
+          ++count;
+        }
+      } else {  // adds the new value first
+        if (!isnan_d(ai)) {
+          asum = __dadd_rn(asum, ai);
+          ++count;
+        }
+        if (!isnan_d(aold)) {
+          asum = __dsub_rn(asum, aold);
+          --count;
+        }
+      }
+      oc[p * inner] = static_cast<T>(count >= mc ? (OP == kMean ? __ddiv_rn(asum, static_cast<double>(count)) : asum) : nan);
+    }
+    return;
+  }
+  if (OP == kVar || OP == kStd) {  // numbagg/moving.py:123-181
+    const long long mc = min_count > 2 ? min_count : 2;
+    double asum = 0.0, asum_sq = 0.0;
+    long long count = 0;
+    for (long long p = 0; p < n; ++p) {
+      const double ai = ld_col(ac + p * inner);
+      if (p >= window) {
+        const double aold = ld_col(ac + (p - window) * inner);
+        if (!isnan_d(aold)) {
+          asum = __dsub_rn(asum, aold);
+          asum_sq = __dsub_rn(asum_sq, __dmul_rn(aold, aold));
+          --count;
+        }
+      }
+      if (!isnan_d(ai)) {
+        asum = __dadd_rn(asum, ai);
+        asum_sq = __dadd_rn(asum_sq, __dmul_rn(ai, ai));
+        ++count;
+      }
+      double r = nan;
+      if (count >= mc) {
+        const double v = __ddiv_rn(__dsub_rn(asum_sq, __ddiv_rn(__dmul_rn(asum, asum), static_cast<double>(count))),
+                                   static_cast<double>(count - 1));
+        r = OP == kStd ? __dsqrt_rn(v) : v;
+      }
+      oc[p * inner] = static_cast<T>(r);
+    }
+    return;
+  }
+  // kCov / kCorr, numbagg/moving.py:184-275
+  const long long mc = OP == kCov ? (min_count > 2 ? min_count : 2) : (min_count > 1 ? min_count : 1);
+  double asum = 0.0, bsum = 0.0, prodsum = 0.0, asum_sq = 0.0, bsum_sq = 0.0;
+  long long count = 0;
+  for (long long p = 0; p < n; ++p) {
+    const double ai = ld_col(ac + p * inner), bi = ld_col(bc + p * inner);
+    if (p >= window) {
+      const double aold = ld_col(ac + (p - window) * inner), bold = ld_col(bc + (p - window) * inner);
+      if (!(isnan_d(aold) || isnan_d(bold))) {
+        asum = __dsub_rn(asum, aold);
+        bsum = __dsub_rn(bsum, bold);
+        prodsum = __dsub_rn(prodsum, __dmul_rn(aold, bold));
+        if (OP == kCorr) {
+          asum_sq = __dsub_rn(asum_sq, __dmul_rn(aold, aold));
+          bsum_sq = __dsub_rn(bsum_sq, __dmul_rn(bold, bold));
+        }
+        --count;
+      }
+    }
+    if (!(isnan_d(ai) || isnan_d(bi))) {
+      asum = __dadd_rn(asum, ai);
+      bsum = __dadd_rn(bsum, bi);
+      prodsum = __dadd_rn(prodsum, __dmul_rn(ai, bi));
+      if (OP == kCorr) {
+        asum_sq = __dadd_rn(asum_sq, __dmul_rn(ai, ai));
+        bsum_sq = __dadd_rn(bsum_sq, __dmul_rn(bi, bi));
+      }
+      ++count;
+    }
+    double r = nan;
+    if (count >= mc) {
+      if (OP == kCov) {
+        r = __ddiv_rn(__dsub_rn(prodsum, __ddiv_rn(__dmul_rn(asum, bsum), static_cast<double>(count))),
+                      static_cast<double>(count - 1));
+      } else {
+        const double cr = __ddiv_rn(1.0, static_cast<double>(count));
+        const double avg_a = __dmul_rn(asum, cr), avg_b = __dmul_rn(bsum, cr);
+        const double var_a = __dsub_rn(__dmul_rn(asum_sq, cr), __dmul_rn(avg_a, avg_a));
+        const double var_b = __dsub_rn(__dmul_rn(bsum_sq, cr), __dmul_rn(avg_b, avg_b));
+        const double cov_ab = __dsub_rn(__dmul_rn(prodsum, cr), __dmul_rn(avg_a, avg_b));
+        const double vv = __dmul_rn(var_a, var_b);
+        if (vv > 0) r = __ddiv_rn(cov_ab, __dsqrt_rn(vv));
+      }
+    }
+    oc[p * inner] = static_cast<T>(r);
+  }
+}
+
 }  // namespace moving
 }  // namespace nbg
 
@@ -667,6 +809,19 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   note_launches(launches);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }
+
+template <int OP, typename T>
+int launch_move_cols(const T* a, const T* b, T* out, long long outer, long long n, long long inner, long long window,
+                     long long min_count, cudaStream_t s) {
+  if (outer < 0 || n < 0 || inner < 0 || window <= 0 || min_count < 0) return kInvalidArgument;
+  if (outer == 0 || n == 0 || inner == 0) return kOk;
+  if (!a || !out || (Traits<OP>::TWO && !b)) return kInvalidArgument;
+  const long long blocks = (outer * inner + 255) / 256;
+  if (blocks > 0x7fffffffLL) return kUnsupported;
+  move_cols_kernel<OP, T><<<static_cast<int>(blocks), 256, 0, s>>>(a, b, out, outer, n, inner, window, min_count);
+  note_launches(1);
+  return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
+}
 }  // namespace
 
 extern "C" {
@@ -707,6 +862,33 @@ NBG_MOVE1(move_var, kVar, double, f64_fp32c, true)
 NBG_MOVE1(move_std, kStd, double, f64_fp32c, true)
 NBG_MOVE2(move_cov, kCov, double, f64_fp32c, true)
 NBG_MOVE2(move_corr, kCorr, double, f64_fp32c, true)
+
+// Along a non-last axis of a C-contiguous array: `outer` blocks of n x `inner` values,
+// scanned along n, one thread per column running numbagg's loop (move_cols_kernel).
+#define NBG_MOVE1_COLS(NAME, OPC, T, SFX)                                                         \
+  int nbg_##NAME##_cols_##SFX(const T* a, T* out, long long outer, long long n, long long inner,   \
+                              long long window, long long min_count, void* stream) {               \
+    return launch_move_cols<OPC, T>(a, nullptr, out, outer, n, inner, window, min_count,            \
+                                    static_cast<cudaStream_t>(stream));                             \
+  }
+#define NBG_MOVE2_COLS(NAME, OPC, T, SFX)                                                         \
+  int nbg_##NAME##_cols_##SFX(const T* a, const T* b, T* out, long long outer, long long n,        \
+                              long long inner, long long window, long long min_count, void* stream) { \
+    return launch_move_cols<OPC, T>(a, b, out, outer, n, inner, window, min_count,                  \
+                                    static_cast<cudaStream_t>(stream));                             \
+  }
+NBG_MOVE1_COLS(move_sum, kSum, double, f64)
+NBG_MOVE1_COLS(move_sum, kSum, float, f32)
+NBG_MOVE1_COLS(move_mean, kMean, double, f64)
+NBG_MOVE1_COLS(move_mean, kMean, float, f32)
+NBG_MOVE1_COLS(move_var, kVar, double, f64)
+NBG_MOVE1_COLS(move_var, kVar, float, f32)
+NBG_MOVE1_COLS(move_std, kStd, double, f64)
+NBG_MOVE1_COLS(move_std, kStd, float, f32)
+NBG_MOVE2_COLS(move_cov, kCov, double, f64)
+NBG_MOVE2_COLS(move_cov, kCov, float, f32)
+NBG_MOVE2_COLS(move_corr, kCorr, double, f64)
+NBG_MOVE2_COLS(move_corr, kCorr, float, f32)
 
 // Ragged series: series s is values[offsets[s] : offsets[s + 1]] (nseries + 1 offsets,
 // on the device), out has the same layout; chunk_len 0 picks the default.

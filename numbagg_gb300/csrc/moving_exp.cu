@@ -34,7 +34,14 @@
 namespace nbg {
 namespace mexp {
 
-enum Op : int { kCount = 0, kMean, kSum, kVar, kStd, kCov, kCorr };
+enum Op : int {
+  kCount = 0, kMean, kSum, kVar, kStd, kCov, kCorr,
+  // The one-pass scan (a scalar alpha): the reference's `weight` state, the sum of
+  // alpha * decay^k over the valid positions, is then alpha times the sum of the
+  // weights decay^k that the statistic scans anyway, so it is not scanned.  Same
+  // statistics, one state fewer (move_exp_nansum keeps its two states).
+  kCountW, kMeanW, kVarW, kStdW, kCovW, kCorrW
+};
 
 template <int OP>
 struct Traits;
@@ -53,6 +60,28 @@ template <>
 struct Traits<kCov> { static constexpr int NS = 6; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
 template <>
 struct Traits<kCorr> { static constexpr int NS = 8; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
+template <>
+struct Traits<kCountW> { static constexpr int NS = 1; static constexpr bool TWO = false; static constexpr int W2 = -1; static constexpr bool PIVOT = false; };
+template <>
+struct Traits<kMeanW> { static constexpr int NS = 2; static constexpr bool TWO = false; static constexpr int W2 = -1; static constexpr bool PIVOT = false; };
+template <>
+struct Traits<kVarW> { static constexpr int NS = 4; static constexpr bool TWO = false; static constexpr int W2 = 3; static constexpr bool PIVOT = true; };
+template <>
+struct Traits<kStdW> { static constexpr int NS = 4; static constexpr bool TWO = false; static constexpr int W2 = 3; static constexpr bool PIVOT = true; };
+template <>
+struct Traits<kCovW> { static constexpr int NS = 5; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
+template <>
+struct Traits<kCorrW> { static constexpr int NS = 7; static constexpr bool TWO = true; static constexpr int W2 = 4; static constexpr bool PIVOT = true; };
+
+// the statistic an op computes, and the op the one-pass scan runs for it
+NBG_HOST_DEVICE constexpr int base_op(int op) {
+  return op == kCountW ? kCount : op == kMeanW ? kMean : op == kVarW ? kVar : op == kStdW ? kStd
+       : op == kCovW ? kCov : op == kCorrW ? kCorr : op;
+}
+NBG_HOST_DEVICE constexpr int scan_op(int op) {
+  return op == kCount ? kCountW : op == kMean ? kMeanW : op == kVar ? kVarW : op == kStd ? kStdW
+       : op == kCov ? kCovW : op == kCorr ? kCorrW : op;
+}
 
 // ---------------------------------------------------------------------------------
 // arithmetic policies
@@ -190,9 +219,45 @@ NBG_DEVICE void contributions(typename N::T x, typename N::T y, typename N::T al
     b[0] = N::mul(x, x); b[1] = x; b[2] = one; b[3] = one; b[4] = alpha;
   } else if (OP == kCov) {  // sum_x1, sum_x2, sum_x1x2, sum_weight, sum_weight_2, weight
     b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one; b[5] = alpha;
-  } else {  // kCorr: + sum_x1_2, sum_x2_2
+  } else if (OP == kCorr) {  // + sum_x1_2, sum_x2_2
     b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one; b[5] = alpha;
     b[6] = N::mul(x, x); b[7] = N::mul(y, y);
+  } else if (OP == kCountW) {  // the same without the weight
+    b[0] = one;
+  } else if (OP == kMeanW) {
+    b[0] = x; b[1] = one;
+  } else if (OP == kVarW || OP == kStdW) {
+    b[0] = N::mul(x, x); b[1] = x; b[2] = one; b[3] = one;
+  } else if (OP == kCovW) {
+    b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one;
+  } else {  // kCorrW
+    b[0] = x; b[1] = y; b[2] = N::mul(x, y); b[3] = one; b[4] = one;
+    b[5] = N::mul(x, x); b[6] = N::mul(y, y);
+  }
+}
+
+// The reference's full state from a weightless one: weight = alpha * sum_weight
+// (the count for move_exp_nancount, the denominator for the mean).
+template <int OP, typename N>
+NBG_DEVICE void with_weight(const typename N::T* s, typename N::T alpha, typename N::T* f) {
+  if (OP == kCountW) {
+    f[0] = s[0]; f[1] = N::mul(alpha, s[0]);
+  } else if (OP == kMeanW) {
+    f[0] = s[0]; f[1] = s[1]; f[2] = N::mul(alpha, s[1]);
+  } else if (OP == kVarW || OP == kStdW) {
+    f[0] = s[0]; f[1] = s[1]; f[2] = s[2]; f[3] = s[3]; f[4] = N::mul(alpha, s[2]);
+  } else if (OP == kCovW) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) f[j] = s[j];
+    f[5] = N::mul(alpha, s[3]);
+  } else if (OP == kCorrW) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) f[j] = s[j];
+    f[5] = N::mul(alpha, s[3]);
+    f[6] = s[5]; f[7] = s[6];
+  } else {
+#pragma unroll
+    for (int j = 0; j < Traits<OP>::NS; ++j) f[j] = s[j];
   }
 }
 
@@ -602,42 +667,103 @@ NBG_DEVICE bool gt0_f64(double x) {  // x > 0 (false for NaN and both zeros)
   return b > 0 && !nan_bits(static_cast<unsigned long long>(b));
 }
 
-// The reference's formulas (finalize(F64, ...)), in the reference's order, with the
-// divisions above: mdiv inside, fdiv for a final quotient (not amplified further).
+NBG_DEVICE bool gt_f64(double x, double y) {  // x > y on the integer pipes (false for NaN)
+  const unsigned long long bx = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long by = static_cast<unsigned long long>(__double_as_longlong(y));
+  if (nan_bits(bx) || nan_bits(by)) return false;
+  return order_key_ieee(x) > order_key_ieee(y);
+}
+NBG_DEVICE unsigned exp_bits(double x) {
+  return static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(x)) >> 52) & 0x7ffu;
+}
+
+// The reference's test bias > 0, bias = 1 - fl(sw2 / S2) with S2 = fl(sw^2)
+// (numbagg/moving_exp.py:150-152), decided without the division: fl(q) < 1 exactly
+// when q < 1 - 2^-54 (the midpoint below 1 rounds to 1, the even neighbour), that is
+// when S2 - sw2 > S2 2^-54.  For S2 in the normal range that difference is exact
+// whenever it decides (sw2 within a factor 2 of S2, Sterbenz) and S2 2^-54 is an
+// exponent shift.  `d` returns S2 - sw2, which is S2 times the reference's bias up to
+// the rounding of that bias.  Other exponents take the reference's expression.
+NBG_DEVICE bool bias_positive(double S2, double sw2, double& d) {
+  d = S2 - sw2;
+  const unsigned e = exp_bits(S2);
+  if (e < 64 || e == 0x7ffu) return gt0_f64(1.0 - sw2 / S2);
+  const double tiny = __longlong_as_double(__double_as_longlong(S2) - (54ll << 52));
+  return gt_f64(d, tiny);
+}
+
+// 1 / b to about an ulp: a float32 reciprocal refined twice (Newton), b's exponent
+// within 120 of 0 (the caller checks)
+NBG_DEVICE double rcp2(double b) {
+  double r = rcp_seed(b);
+  r = fma(fma(-b, r, 1.0), r, r);
+  return fma(fma(-b, r, 1.0), r, r);
+}
+
+// The reference's statistics (numbagg/moving_exp.py:142-156, :265-273, :318-335) with
+// the divisions cleared: var = (sw sum_x2 - sum_x^2) / (sw^2 - sw2) is var_biased / bias
+// multiplied through by sw^2, cov the same, and the correlation's three centred sums
+// take one reciprocal of sw.  Every cancellation keeps the reference's conditioning
+// (the same differences of the same products), the one quotient is taken nearly
+// correctly rounded (mdiv), and the NaN decisions are the reference's (bias_positive,
+// weight >= min_weight, the denominator > 0).  Exponents outside the ranges those forms
+// assume take the reference's expressions with IEEE divisions.
+template <int OP>
+NBG_DEVICE double finalize_ref(const double* s, double min_weight) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  if (OP == kVar || OP == kStd) {
+    const double m = s[1] / s[2];
+    const double vb = s[0] / s[2] - m * m;
+    const double bias = 1.0 - s[3] / (s[2] * s[2]);
+    if (!(s[4] >= min_weight && bias > 0)) return nan;
+    const double v = vb / bias;
+    return OP == kStd ? sqrt(v) : v;
+  }
+  if (OP == kCov) {
+    const double cb = (s[2] - s[0] * s[1] / s[3]) / s[3];
+    const double bias = 1.0 - s[4] / (s[3] * s[3]);
+    return (s[5] >= min_weight && bias > 0) ? cb / bias : nan;
+  }
+  const double cov = s[2] - s[0] * s[1] / s[3];
+  const double v1 = s[6] - s[0] * s[0] / s[3];
+  const double v2 = s[7] - s[1] * s[1] / s[3];
+  const double bias = 1.0 - s[4] / (s[3] * s[3]);
+  if (!(s[5] >= min_weight && bias > 0)) return nan;
+  const double den = sqrt(v1 * v2);
+  return den > 0 ? cov / den : nan;
+}
+
 template <int OP>
 NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   if (OP == kCount) return ge_f64(s[1], min_weight) ? s[0] : nan;
   if (OP == kMean) return ge_f64(s[2], min_weight) ? fdiv(s[0], s[1]) : nan;
   if (OP == kSum) return (ge_f64(s[1], min_weight) && seen) ? s[0] : nan;
-  // the variance family: the bias 1 - sw2 / sw^2 can cancel to a few ulps, so the
-  // statistic can be many times its natural scale and every quotient and root here is
-  // taken nearly correctly rounded (mdiv, sqrt)
-  if (OP == kVar || OP == kStd) {  // numbagg/moving_exp.py:142-156
-    const double m = mdiv(s[1], s[2]);
-    const double var_biased = mdiv(s[0], s[2]) - m * m;
-    const double bias = 1.0 - mdiv(s[3], s[2] * s[2]);
-    if (ge_f64(s[4], min_weight) && gt0_f64(bias)) {
-      const double v = mdiv(var_biased, bias);
-      return OP == kStd ? sqrt(v) : v;
-    }
-    return nan;
+  constexpr int W = (OP == kVar || OP == kStd) ? 2 : 3;  // sum_weight; W + 1 sum_weight_2, W + 2 weight
+  const unsigned ew = exp_bits(s[W]);
+  if (ew < 1023 - 100 || ew > 1023 + 100) return finalize_ref<OP>(s, min_weight);
+  double d;
+  if (!(ge_f64(s[W + 2], min_weight) && bias_positive(s[W] * s[W], s[W + 1], d))) return nan;
+  if (OP == kVar || OP == kStd) {
+    const double num = fma(s[0], s[2], -(s[1] * s[1]));
+    const unsigned en = exp_bits(num);
+    if (en == 0x7ffu || en > 1023 + 900) return finalize_ref<OP>(s, min_weight);
+    const double v = mdiv(num, d);
+    return OP == kStd ? sqrt(v) : v;
   }
-  if (OP == kCov) {  // numbagg/moving_exp.py:265-273
-    const double cov_biased = mdiv(s[2] - mdiv(s[0] * s[1], s[3]), s[3]);
-    const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
-    return (ge_f64(s[5], min_weight) && gt0_f64(bias)) ? mdiv(cov_biased, bias) : nan;
+  if (OP == kCov) {
+    const double num = fma(s[2], s[3], -(s[0] * s[1]));
+    const unsigned en = exp_bits(num);
+    if (en == 0x7ffu || en > 1023 + 900) return finalize_ref<OP>(s, min_weight);
+    return mdiv(num, d);
   }
-  // kCorr, numbagg/moving_exp.py:318-335
-  const double cov = s[2] - mdiv(s[0] * s[1], s[3]);
-  const double var1 = s[6] - mdiv(s[0] * s[0], s[3]);
-  const double var2 = s[7] - mdiv(s[1] * s[1], s[3]);
-  const double bias = 1.0 - mdiv(s[4], s[3] * s[3]);
-  if (ge_f64(s[5], min_weight) && gt0_f64(bias)) {
-    const double den = sqrt(var1 * var2);
-    return gt0_f64(den) ? mdiv(cov, den) : nan;
-  }
-  return nan;
+  // kCorr
+  const double r = rcp2(s[3]);
+  const double cov = fma(-(s[0] * s[1]), r, s[2]);
+  const double v1 = fma(-(s[0] * s[0]), r, s[6]);
+  const double v2 = fma(-(s[1] * s[1]), r, s[7]);
+  const double den = sqrt(v1 * v2);
+  return gt0_f64(den) ? mdiv(cov, den) : nan;
 }
 
 // Double-float finalisation of the one-pass scan: min_weight converted once per
@@ -664,47 +790,43 @@ template <int OP>
 NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {
   using namespace dfl;
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
-  const df one{1.0f, 0.0f};
   if (OP == kCount) return df_ge_df(s[1], mw) ? df_out(s[0]) : nan;
   if (OP == kMean) return df_ge_df(s[2], mw) ? df_out(df_div_fast(s[0], s[1])) : nan;
   if (OP == kSum) return (df_ge_df(s[1], mw) && seen) ? df_out(s[0]) : nan;
+  // the variance family with the divisions cleared as in finalize_fast: var =
+  // (sw sum_x2 - sum_x^2) / (sw^2 - sw2), the bias test sw^2 > sw2, and the correlation
+  // from the centred sums multiplied through by sw (on pivoted values, so the products
+  // stay far inside float32's range)
   if (OP == kVar || OP == kStd) {
-    const df rw = df_div_fast(one, s[2]);
-    const df m = df_mul(s[1], rw);
-    const df var_biased = df_sub(df_mul(s[0], rw), df_mul(m, m));
-    const df bias = df_sub(one, df_mul(s[3], df_mul(rw, rw)));
-    if (df_ge_df(s[4], mw) && df_pos(bias)) {
-      const df v = df_div_fast(var_biased, bias);
-      if (OP == kVar) return df_out(v);
-      if (v.hi < 0.0f) return nan;
-      return v.hi == 0.0f ? 0.0 : df_out(df_sqrt(v));
-    }
-    return nan;
+    const df den = df_sub(df_mul(s[2], s[2]), s[3]);
+    if (!(df_ge_df(s[4], mw) && df_pos(den))) return nan;
+    const df v = df_div_fast(df_sub(df_mul(s[0], s[2]), df_mul(s[1], s[1])), den);
+    if (OP == kVar) return df_out(v);
+    if (v.hi < 0.0f) return nan;
+    return v.hi == 0.0f ? 0.0 : df_out(df_sqrt(v));
   }
-  const df rw = df_div_fast(one, s[3]);
-  const df bias = df_sub(one, df_mul(s[4], df_mul(rw, rw)));
-  if (OP == kCov) {
-    const df cov_biased = df_mul(df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw)), rw);
-    return (df_ge_df(s[5], mw) && df_pos(bias)) ? df_out(df_div_fast(cov_biased, bias)) : nan;
-  }
-  const df cov = df_sub(s[2], df_mul(df_mul(s[0], s[1]), rw));
-  const df var1 = df_sub(s[6], df_mul(df_mul(s[0], s[0]), rw));
-  const df var2 = df_sub(s[7], df_mul(df_mul(s[1], s[1]), rw));
-  if (df_ge_df(s[5], mw) && df_pos(bias)) {
-    const df vv = df_mul(var1, var2);
-    if (!df_pos(vv)) return nan;
-    return df_out(df_div_fast(cov, df_sqrt(vv)));
-  }
-  return nan;
+  const df den = df_sub(df_mul(s[3], s[3]), s[4]);
+  if (!(df_ge_df(s[5], mw) && df_pos(den))) return nan;
+  if (OP == kCov) return df_out(df_div_fast(df_sub(df_mul(s[2], s[3]), df_mul(s[0], s[1])), den));
+  const df cov = df_sub(df_mul(s[2], s[3]), df_mul(s[0], s[1]));
+  const df var1 = df_sub(df_mul(s[6], s[3]), df_mul(s[0], s[0]));
+  const df var2 = df_sub(df_mul(s[7], s[3]), df_mul(s[1], s[1]));
+  const df vv = df_mul(var1, var2);
+  if (!df_pos(vv)) return nan;
+  return df_out(df_div_fast(cov, df_sqrt(vv)));
 }
 
 template <int OP>
-NBG_DEVICE double finalize_scan(F64, const double* s, int seen, double min_weight, double) {
-  return finalize_fast<OP>(s, seen, min_weight);
+NBG_DEVICE double finalize_scan(F64, const double* s, int seen, double min_weight, double, double alpha) {
+  double f[Traits<base_op(OP)>::NS];
+  with_weight<OP, F64>(s, alpha, f);
+  return finalize_fast<base_op(OP)>(f, seen, min_weight);
 }
 template <int OP>
-NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double, dfl::df mw) {
-  return finalize_dfast<OP>(s, seen, mw);
+NBG_DEVICE double finalize_scan(DF, const dfl::df* s, int seen, double, dfl::df mw, dfl::df alpha) {
+  dfl::df f[Traits<base_op(OP)>::NS];
+  with_weight<OP, DF>(s, alpha, f);
+  return finalize_dfast<base_op(OP)>(f, seen, mw);
 }
 
 template <typename N>
@@ -753,6 +875,17 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
   const V d_warp = pow_n<N>(pow_n<N>(d8, 32), warp), dd_warp = pow_n<N>(pow_n<N>(dd8, 32), warp);
   const V d_start = N::mul(d_warp, d_lane), dd_start = N::mul(dd_warp, dd_lane);  // d^(8 tid)
   const V d_tile = pow_n<N>(d8, NT), dd_tile = pow_n<N>(dd8, NT);
+  // the warp scan's factors (d^8)^(2^k), k = 0..5, once per CTA (float64: a multiply
+  // per level and tile saved on the FP64 pipe; double-float squares them per tile, as
+  // the registers for a table would spill there)
+  V pw1[6], pw2[6];
+  pw1[0] = d8;
+  pw2[0] = dd8;
+#pragma unroll
+  for (int k = 1; k < 6; ++k) {
+    pw1[k] = N::mul(pw1[k - 1], pw1[k - 1]);
+    pw2[k] = N::mul(pw2[k - 1], pw2[k - 1]);
+  }
 
   for (;;) {
     if (tid == 0) tile_smem = claim_tile(ws.hdr);
@@ -815,7 +948,8 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
     // ---- warp scan: S_lane = sum over lanes l' <= lane of (d^8)^(lane - l') s_l' ----
     V f1 = d8, f2 = dd8;
 #pragma unroll
-    for (int dl = 1; dl < 32; dl <<= 1) {
+    for (int lvl = 0; lvl < 5; ++lvl) {
+      const int dl = 1 << lvl;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         const V up = shfl_up_num(s[j], dl);
@@ -823,8 +957,13 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
       }
       const int us = __shfl_up_sync(0xffffffffu, seen, dl);
       if (lane >= dl) seen |= us;
-      f1 = N::mul(f1, f1);
-      f2 = N::mul(f2, f2);
+      if constexpr (N::kDF) {
+        f1 = N::mul(f1, f1);
+        f2 = N::mul(f2, f2);
+      } else {
+        f1 = pw1[lvl + 1];
+        f2 = pw2[lvl + 1];
+      }
     }
     // exclusive prefix within the warp
     V e[NS];
@@ -901,21 +1040,13 @@ __global__ void __launch_bounds__(NT) exp_scan_kernel(const T* __restrict__ a, c
       load(k, x, y, valid);
       V bj[NS];
       contributions<OP, N>(x, y, al, bj);
-      // the variance family takes the reference's update (a rounded multiply, then a
-      // rounded add): its bias 1 - sw2 / sw^2 can cancel to a few ulps and amplify any
-      // other rounding; count, mean and sum use one multiply-add
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
-        if (Traits<OP>::PIVOT) {
-          s[j] = N::mul(s[j], (j == W2) ? dd : d);
-          if (valid) s[j] = N::add(s[j], bj[j]);
-        } else {
-          if (!valid) bj[j] = N::zero();
-          s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
-        }
+        if (!valid) bj[j] = N::zero();
+        s[j] = N::fma(s[j], (j == W2) ? dd : d, bj[j]);
       }
       seen |= valid ? 1 : 0;
-      res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight, mw_n));
+      res[k] = static_cast<T>(finalize_scan<OP>(N(), s, seen, min_weight, mw_n, al));
     }
     __syncthreads();  // every thread has read its run: the stage takes the outputs
 #pragma unroll
@@ -1053,12 +1184,13 @@ int launch_exp_scan(const T* a, const T* b, double alpha_scalar, double min_weig
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (per_sm == 0) {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exp_scan_kernel<OP, T, N>, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exp_scan_kernel<scan_op(OP), T, N>, NT, 0);
     per_sm = nb > 0 ? nb : 1;
   }
   const long long cap = static_cast<long long>(sms) * per_sm;
   const int grid = static_cast<int>(tiles < cap ? tiles : cap);
-  exp_scan_kernel<OP, T, N><<<grid, NT, 0, s>>>(a, b, alpha_scalar, min_weight, out, rows, n, tpr, ws, lb, pivots);
+  exp_scan_kernel<scan_op(OP), T, N><<<grid, NT, 0, s>>>(a, b, alpha_scalar, min_weight, out, rows, n, tpr, ws, lb,
+                                                          pivots);
   note_launches(launches);
   return cudaGetLastError() == cudaSuccess ? kOk : kLaunchError;
 }

@@ -59,10 +59,15 @@ def _move(name: str, arrs, window, min_count, axis, precision="f64"):
     if len(tensors) > 1:
         tensors = list(torch.broadcast_tensors(*tensors))
         dtype = _host.float_compute_dtype(torch.promote_types(tensors[0].dtype, tensors[1].dtype))
+    tensors = [t.to(dtype) for t in tensors]
+    if precision == "f64":
+        cols_out = _move_columns(name, tensors, window, min_count, axis)
+        if cols_out is not None:
+            return restore(cols_out)
     flats = []
     shape = None
     for t in tensors:
-        f, shape = _host.rows_last(t.to(dtype), axis)
+        f, shape = _host.rows_last(t, axis)
         flats.append(f)
     rows, n = flats[0].shape
     out = torch.empty((rows, n), dtype=dtype, device=a.device)
@@ -85,6 +90,30 @@ def _move(name: str, arrs, window, min_count, axis, precision="f64"):
         ]
         _lib.check(fn(*args), name)
     return restore(_host.restore_axis(out, shape, axis))
+
+
+def _move_columns(name, tensors, window, min_count, axis):
+    """A non-last axis of contiguous arrays: one thread per column runs numbagg's loop
+    down it in place (no copy), bit for bit the reference's float64 arithmetic.  None
+    when the layout does not apply."""
+    cols = _host.column_layout(tensors[0], axis)
+    if cols is None or any(t.shape != tensors[0].shape or not t.is_contiguous() for t in tensors):
+        return None
+    outer, n, inner = cols
+    out = torch.empty_like(tensors[0])
+    if out.numel():
+        fn = getattr(_lib.lib(), f"nbg_{name}_cols_{_host.FLOAT_SFX[out.dtype]}")
+        args = [t.data_ptr() for t in tensors] + [
+            out.data_ptr(),
+            outer,
+            n,
+            inner,
+            window,
+            min_count,
+            _host.stream(out.device),
+        ]
+        _lib.check(fn(*args), name)
+    return out
 
 
 def move_sum(arr, /, *, window, min_count=None, axis=-1, precision="f64"):

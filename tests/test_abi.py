@@ -61,6 +61,9 @@ def test_invalid_arguments_are_rejected_before_launch(lib):
     assert lib.nbg_move_exp_nanmean_f64(null, null, 0.5, 7, 0.0, null, 1, 10, null, 0, null) == 1
     assert lib.nbg_group_nansum_f64_i32(null, null, null, -1, 10, 4, 1, null, 0, null) == 1
     assert lib.nbg_move_covmatrix_f64(null, null, 1, 10, 3, 0, 1, null) == 1
+    assert lib.nbg_move_std_cols_f64(null, null, 1, 10, 4, 0, 3, null) == 1
+    assert lib.nbg_move_corr_cols_f32(null, null, null, 1, 10, 4, 3, -1, null) == 1
+    assert lib.nbg_move_mean_cols_f64(null, null, 0, 10, 4, 3, 3, null) == 0
     # empty problems succeed without work
     assert lib.nbg_move_mean_f64(null, null, 0, 10, 3, 3, null, 0, null) == 0
     assert lib.nbg_ffill_f32(null, null, 3, 0, 2, null, 0, null) == 0

@@ -159,3 +159,36 @@ def test_large_row_sum_and_determinism():
     mag = oracle.aggregate("nansum", np.abs(a), axis=1, ext=True)
     assert (np.abs(got - ext) / mag).max() <= 1e-12
     np.testing.assert_array_equal(nb.nanargmax(a, axis=1), oracle.aggregate("nanargmax", a, axis=1))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int64])
+def test_middle_axes_in_place(dtype):
+    # consecutive reduced axes that are not last run in place through their stride
+    # (one warp of consecutive outputs per CTA, chunks of the reduced extent)
+    warnings.simplefilter("ignore")
+    a = _data(dtype, seed=12, shape=(4, 40, 50, 64))
+    for name in EXACT + ["nansum"]:
+        for axis in ((1, 2), 0, (0, 1, 2)):
+            want, err = _ok_axis(name, a, axis)
+            if err is not None:
+                continue
+            got = getattr(nb, name)(a, axis=axis)
+            if name == "nansum" and dtype != np.int64:
+                mag = oracle.aggregate(name, np.abs(np.nan_to_num(a, posinf=0, neginf=0)), axis=axis)
+                mag = np.asarray(mag, dtype=np.float64)
+                g64, w64 = np.asarray(got, dtype=np.float64), np.asarray(want, dtype=np.float64)
+                ok = np.isfinite(w64)
+                assert np.array_equal(g64[~ok], w64[~ok], equal_nan=True)
+                err = np.abs(g64 - w64)[ok] / np.maximum(mag[ok], 1e-300)
+                assert err.max(initial=0.0) <= (1e-12 if dtype == np.float64 else 2e-6), (axis, err.max(initial=0.0))
+            else:
+                np.testing.assert_array_equal(got, want, err_msg=f"{name} axis={axis}")
+    # a long reduced axis over few outputs: many chunks per warp of outputs
+    rng = np.random.default_rng(13)
+    b = rng.standard_normal((400_000, 64))
+    b[rng.random(b.shape) < 0.05] = np.nan
+    for name in ("nanmean", "nanvar"):
+        got = getattr(nb, name)(b, axis=0)
+        ext = oracle.aggregate(name, b, axis=0, ext=True)
+        assert (np.abs(got - ext) / np.abs(ext)).max() <= 1e-12, name
+    np.testing.assert_array_equal(nb.nanargmin(b, axis=0), oracle.aggregate("nanargmin", b, axis=0))

@@ -1,9 +1,9 @@
 """A scanned axis that is not the last one (numbagg's gufuncs take such strided core
 axes directly, numbagg/decorators.py:340-341, :409-414, :480-487).
 
-For C-contiguous arrays with enough columns the fills and the exponentially weighted
-family run one thread per column, in place, instead of moving the axis last and
-copying.  That kernel repeats numbagg's loop operation for operation, so float64 (and
+For C-contiguous arrays with enough columns the fills, the moving windows and the
+exponentially weighted family run one thread per column, in place, instead of moving
+the axis last and copying.  That kernel repeats numbagg's loop operation for operation, so float64 (and
 float32 with a float32 alpha) results must equal the oracle bit for bit; the
 FP32-compensated form keeps its stated 2e-6.  The last tests make the calls that
 xarray's rolling_exp and flox's grouped reductions make.
@@ -45,6 +45,36 @@ def test_fill_non_last_axis(fname, dtype, shape, axis):
         got = getattr(nb, fname)(xt, limit=limit, axis=axis).cpu().numpy()
         want = oracle.fill(fname, x, limit=limit, axis=axis)
         assert_bit_equal(got, want, f"{fname} axis={axis} limit={limit}")
+
+
+MOVE = ["move_sum", "move_mean", "move_var", "move_std", "move_cov", "move_corr"]
+
+
+@pytest.mark.parametrize("fname", MOVE)
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("shape,axis", [((1500, 2500), 0), ((4, 700, 1024), 1)])
+def test_move_non_last_axis_bit_exact(fname, dtype, shape, axis):
+    x = _data(shape, 41, dtype=dtype)
+    y = _data(shape, 42, dtype=dtype) if fname in ("move_cov", "move_corr") else None
+    x[tuple(s // 3 for s in shape)] = np.inf  # the reference's running sums never recover
+    func = getattr(nb, fname)
+    xt = torch.from_numpy(x).cuda()
+    assert _host.column_layout(xt, axis) is not None  # the in-place column path
+    args = (xt,) if y is None else (xt, torch.from_numpy(y).cuda())
+    for window, min_count in ((1, None), (7, 3), (300, 150)):
+        got = func(*args, window=window, min_count=min_count, axis=axis).cpu().numpy()
+        want = oracle.move(fname, x, y, window=window, min_count=min_count, axis=axis)
+        assert_bit_equal(got, want, f"{fname} {np.dtype(dtype).name} w={window}")
+
+
+def test_move_non_last_axis_fp32c_keeps_its_bound():
+    # the compensated form runs the rows kernels (moved axis); same 2e-6 bar
+    x = 1e6 + _data((2000, 2100), 43)
+    got = nb.move_std(x, window=50, min_count=25, axis=0, precision="fp32c")
+    ext = oracle.move("move_std", x, window=50, min_count=25, axis=0, ext=True)
+    m = ~np.isnan(ext)
+    assert np.array_equal(np.isnan(got), np.isnan(ext))
+    assert np.max(np.abs(got[m] - ext[m]) / np.abs(ext[m])) <= 2e-6
 
 
 @pytest.mark.parametrize("fname", MOVE_EXP)
