@@ -48,6 +48,12 @@ NBG_DEVICE df df_add(df x, df y) {  // the accurate ("IEEE") double-float sum
   return fast_two_sum(s.hi, e);
 }
 NBG_DEVICE df df_neg(df x) { return df{-x.hi, -x.lo}; }
+// the cheaper ("sloppy") sum: error about 2^-44 of |x| + |y| (the accurate one above is
+// within a few ulps of the result even when x + y cancels)
+NBG_DEVICE df df_add_fast(df x, df y) {
+  const df s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, __fadd_rn(__fadd_rn(s.lo, x.lo), y.lo));
+}
 NBG_DEVICE df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
 NBG_DEVICE df df_mul(df x, df y) {
   const df p = two_prod(x.hi, y.hi);
@@ -252,4 +258,54 @@ NBG_DEVICE s256 ssub(const s256& x, const s256& y) {
 }
 
 }  // namespace dfl
+
+// a float64 as a double-float with integer instructions (the FP64 pipe converts slowly
+// on this GPU): the top 24 bits of the mantissa as hi, the next 29 rounded into lo
+// (about 48 bits in all); infinities and NaN keep their class, values beyond float32's
+// range overflow to infinity and values below its normal range round through float32.
+NBG_DEVICE dfl::df df_from_f64(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0x000fffffffffffffull;
+  if (e == 0x7ff) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u | (m ? 0x400000u : 0u))), 0.0f};
+  const int E = e - 1023;
+  if (e == 0 || E < -126) {  // below float32's normal range: a float32 rounding of it
+    const float h = __double2float_rn(x);
+    return dfl::df{h, __double2float_rn(x - static_cast<double>(h))};
+  }
+  if (E > 127) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u)), 0.0f};
+  const unsigned long long M = m | 0x0010000000000000ull;
+  const float hi = __int_as_float(static_cast<int>(sign | (static_cast<unsigned>(E + 127) << 23) |
+                                                  static_cast<unsigned>((M >> 29) & 0x7fffffu)));
+  const unsigned rem = static_cast<unsigned>(M & ((1ull << 29) - 1));
+  float lo = 0.0f;
+  if (rem && E - 52 >= -126) {
+    lo = __fmul_rn(__uint2float_rn(rem), dfl::pow2f(E - 52));
+    if (sign) lo = -lo;
+  }
+  return dfl::fast_two_sum(hi, lo);
+}
+
+// a float32 widened to float64 from its bit pattern (the FP64 pipe executes the
+// conversion instruction, slowly on this GPU); zeros keep their sign, subnormals,
+// infinities and NaN take the conversion instruction
+NBG_DEVICE double widen_f32(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned ef = (b >> 23) & 0xffu;
+  if ((b << 1) == 0u) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(b >> 31) << 63));
+  if (ef == 0u || ef == 0xffu) return static_cast<double>(x);
+  const unsigned long long sign = static_cast<unsigned long long>(b >> 31) << 63;
+  const unsigned long long e = static_cast<unsigned long long>(ef - 127u + 1023u);
+  return __longlong_as_double(static_cast<long long>(sign | (e << 52) | (static_cast<unsigned long long>(b & 0x7fffffu) << 29)));
+}
+// hi + lo rounded to float64: two exact widenings and one float64 add
+NBG_DEVICE double df_to_double(dfl::df x) { return widen_f32(x.hi) + widen_f32(x.lo); }
+// a nonnegative count below 2^31 as a double-float, exactly
+NBG_DEVICE dfl::df df_of_int(long long c) {
+  const int ci = static_cast<int>(c);
+  const float hi = __int2float_rn(ci);
+  return dfl::df{hi, __int2float_rn(ci - __float2int_rz(hi))};
+}
+
 }  // namespace nbg

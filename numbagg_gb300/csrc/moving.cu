@@ -417,7 +417,8 @@ __global__ void __launch_bounds__(NT, MoveOcc<OP>::value) move_kernel(const T* _
                                                      T* __restrict__ out, Layout lay, long long window,
                                                      long long min_count, long long chunk_len,
                                                      const double* __restrict__ rcp, long long rcp_n,
-                                                     long long* __restrict__ first_bad) {
+                                                     long long* __restrict__ first_bad,
+                                                     const unsigned* __restrict__ only_rows) {
   constexpr int NS = Traits<OP>::NS;
   constexpr bool TWO = Traits<OP>::TWO;
   typedef typename BitsOf<T>::type B;
@@ -436,6 +437,9 @@ __global__ void __launch_bounds__(NT, MoveOcc<OP>::value) move_kernel(const T* _
   for (long long id = blockIdx.x; id < items; id += gridDim.x) {
   const Item it = layout_item(lay, id);
   const long long row = it.row, n = it.len;
+  // only_rows: recompute just the rows the double-float scan flagged (the whole CTA
+  // takes the same branch, before any barrier)
+  if (only_rows && only_rows[row] == 0u) continue;
   const long long c0 = it.index * chunk_len, c1 = min(n, c0 + chunk_len);
   const B* ar = as_bits(a) + it.base;
   const B* br = TWO ? as_bits(b) + it.base : ar;
@@ -549,11 +553,14 @@ __global__ void __launch_bounds__(NT, MoveOcc<OP>::value) move_kernel(const T* _
 
 // reciprocal table and per-row first infinity, once per call
 __global__ void move_setup_kernel(double* __restrict__ rcp, long long rcp_n, long long* __restrict__ first_bad,
-                                  long long rows) {
+                                  long long rows, unsigned* __restrict__ flags) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   const long long t0 = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   for (long long c = t0; c <= rcp_n; c += stride) rcp[c] = c ? 1.0 / static_cast<double>(c) : 0.0;
-  for (long long r = t0; r < rows; r += stride) first_bad[r] = LLONG_MAX;
+  for (long long r = t0; r < rows; r += stride) {
+    first_bad[r] = LLONG_MAX;
+    if (flags) flags[r] = 0u;
+  }
 }
 
 // The reference never recovers from an infinity (inf - inf = NaN in its running sums):
@@ -570,6 +577,348 @@ __global__ void move_poison_kernel(T* __restrict__ out, Layout lay, long long wi
     for (long long i = (from < n ? from : n) + threadIdx.x; i < n; i += blockDim.x) out[base + i] = nan;
   }
 }
+
+// ---------------------------------------------------------------------------------
+// FP32-compensated form, one pass: double-float window sums
+// ---------------------------------------------------------------------------------
+// The window state at i (the count and the sums: x; or y = x - p, y^2; ya, yb, ya yb,
+// ya^2, yb^2, with p the row's pivot, its first finite value) is the prefix sum of the
+// differences d_i = c(x_i) - c(x_{i-w}).  Rows are cut into tiles of 1024 positions,
+// claimed row-interleaved.  A tile stages its entering and leaving values; each thread
+// folds the differences of 8 consecutive positions in double-float (about 48 bits, on
+// the FP32 pipes); a warp scan and a fold over the warps give the tile's total; lane 0
+// chains it to the inclusive prefix that the row's previous tile published (a bounded
+// wait) and publishes its own, so the result does not depend on timing; each thread
+// then replays its positions from the state entering them and finalises.  Every value
+// is read once as entering and once as leaving (from L2 while the window is short).
+// Rows holding an infinity or a value outside the range these sums keep to the
+// stated bound (|x| or |y| of 2^50 and more, or a nonzero |y| below 2^-60; |x| outside
+// [2^-100, 2^100] for sums and means) are flagged and recomputed by move_kernel's exact
+// sums, which also carry the reference's infinity semantics.
+namespace dsc {
+constexpr int NT = 128;
+constexpr int KT = 8;
+constexpr int TILE = NT * KT;
+constexpr int SPAD = TILE + TILE / KT;
+NBG_DEVICE int spad(int p) { return p + p / KT; }
+
+template <int NS>
+struct St {
+  dfl::df s[NS];
+  int cnt;
+  int pad;
+};
+template <int NS>
+NBG_DEVICE St<NS> st_zero() {
+  St<NS> r;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) r.s[j] = dfl::df{0.0f, 0.0f};
+  r.cnt = 0;
+  r.pad = 0;
+  return r;
+}
+template <int NS>
+NBG_DEVICE St<NS> st_add(const St<NS>& a, const St<NS>& b) {
+  St<NS> r;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) r.s[j] = dfl::df_add(a.s[j], b.s[j]);
+  r.cnt = a.cnt + b.cnt;
+  r.pad = 0;
+  return r;
+}
+template <int NS>
+NBG_DEVICE St<NS> st_shfl_up(const St<NS>& v, int d) {
+  St<NS> r;
+#pragma unroll
+  for (int j = 0; j < NS; ++j)
+    r.s[j] = dfl::df{__shfl_up_sync(0xffffffffu, v.s[j].hi, d), __shfl_up_sync(0xffffffffu, v.s[j].lo, d)};
+  r.cnt = __shfl_up_sync(0xffffffffu, v.cnt, d);
+  r.pad = 0;
+  return r;
+}
+
+// |x| within [2^-100, 2^100] or zero (sums, means); |x| below 2^50 (the rest)
+template <bool VL>
+NBG_DEVICE bool raw_ok(unsigned long long b) {
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  if (VL) return e < 1023 + 50;
+  return (b << 1) == 0 || (e >= 1023 - 100 && e <= 1023 + 100);
+}
+// a pivoted value zero or at least 2^-60 in magnitude
+NBG_DEVICE bool piv_ok(double y) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(y));
+  return (b << 1) == 0 || static_cast<int>((b >> 52) & 0x7ff) >= 1023 - 60;
+}
+
+// One position's contributions (the value pair is valid): x for sums and means; the
+// pivoted y = x - p (one float64 subtraction, exact for values near the pivot), y^2
+// (variance); ya, yb, ya yb (covariance); + ya^2, yb^2 (correlation).  `ok` turns
+// false when a value is outside the range above.
+template <int OP>
+NBG_DEVICE void contrib(unsigned long long xb, unsigned long long yb, double px, double py, dfl::df* c, bool& ok) {
+  constexpr bool VL = Traits<OP>::VARLIKE, TWO = Traits<OP>::TWO;
+  using namespace dfl;
+  ok = ok && raw_ok<VL>(xb) && (!TWO || raw_ok<VL>(yb));
+  if (!VL) {
+    c[0] = df_from_f64(__longlong_as_double(static_cast<long long>(xb)));
+    return;
+  }
+  const double xd = __longlong_as_double(static_cast<long long>(xb)) - px;
+  ok = ok && piv_ok(xd);
+  const df x = df_from_f64(xd);
+  if (OP == kVar || OP == kStd) {
+    c[0] = x;
+    c[1] = df_mul(x, x);
+    return;
+  }
+  const double yd = __longlong_as_double(static_cast<long long>(yb)) - py;
+  ok = ok && piv_ok(yd);
+  const df y = df_from_f64(yd);
+  c[0] = x;
+  c[1] = y;
+  c[2] = df_mul(x, y);
+  if (OP == kCorr) {
+    c[3] = df_mul(x, x);
+    c[4] = df_mul(y, y);
+  }
+}
+
+// s / c for a count c >= 1 (exact in float32 below 2^24)
+NBG_DEVICE dfl::df df_div_count(dfl::df s, long long c) {
+  using namespace dfl;
+  const float cf = static_cast<float>(c);
+  if (c < (1ll << 24)) {
+    const float q1 = __fdiv_rn(s.hi, cf);
+    const df r = df_sub(s, two_prod(q1, cf));
+    return fast_two_sum(q1, __fdiv_rn(r.hi, cf));
+  }
+  const double cd = static_cast<double>(c);
+  return df_div(s, df_from_f64(cd));
+}
+NBG_DEVICE dfl::df df_of_count(long long c) {
+  return c < (1ll << 31) ? df_of_int(c) : df_from_f64(static_cast<double>(c));
+}
+NBG_DEVICE double df_out(dfl::df x) {
+  if (!isfinite(x.hi)) return static_cast<double>(x.hi);
+  return df_to_double(x);
+}
+
+// the reference's statistics from the window sums (numbagg/moving.py:12-275), with the
+// common factors cancelled: var = (c S_yy - S_y^2) / (c (c - 1)), the same for the
+// covariance, corr = N_ab / sqrt(N_aa N_bb)
+template <int OP>
+NBG_DEVICE double finalize_d(const St<Traits<OP>::NS>& st, long long min_count) {
+  using namespace dfl;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const long long c = st.cnt;
+  if (OP == kSum) return c >= min_count ? df_out(st.s[0]) : nan;
+  if (OP == kMean) return c >= (min_count > 1 ? min_count : 1) ? df_out(df_div_count(st.s[0], c)) : nan;
+  const df cd = df_of_count(c);
+  if (OP == kVar || OP == kStd || OP == kCov) {
+    if (c < (min_count > 2 ? min_count : 2)) return nan;
+    const df num = OP == kCov ? df_sub(df_mul(cd, st.s[2]), df_mul(st.s[0], st.s[1]))
+                              : df_sub(df_mul(cd, st.s[1]), df_mul(st.s[0], st.s[0]));
+    const long long cc = c * (c - 1);
+    const df v = cc < (1ll << 24) ? df_div_count(num, cc) : df_div_count(df_div_count(num, c), c - 1);
+    if (OP != kStd) return df_out(v);
+    if (v.hi < 0.0f) return nan;
+    return v.hi == 0.0f ? 0.0 : df_out(df_sqrt(v));
+  }
+  if (c < (min_count > 1 ? min_count : 1)) return nan;
+  const df naa = df_sub(df_mul(cd, st.s[3]), df_mul(st.s[0], st.s[0]));
+  const df nbb = df_sub(df_mul(cd, st.s[4]), df_mul(st.s[1], st.s[1]));
+  const df nab = df_sub(df_mul(cd, st.s[2]), df_mul(st.s[0], st.s[1]));
+  const df vv = df_mul(naa, nbb);
+  if (!(vv.hi > 0.0f || (vv.hi == 0.0f && vv.lo > 0.0f))) return nan;
+  return df_out(df_div(nab, df_sqrt(vv)));
+}
+
+// the row's pivot: its first finite value (0 when it has none)
+template <typename T>
+__global__ void dsc_pivot_kernel(const T* __restrict__ a, const T* __restrict__ b, long long rows, long long n,
+                                 double* __restrict__ pivots) {
+  const int lane = threadIdx.x & 31;
+  const long long row = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (row >= rows) return;
+  for (int w = 0; w < (b ? 2 : 1); ++w) {
+    const T* r = (w ? b : a) + row * n;
+    double pv = 0.0;
+    for (long long base = 0; base < n; base += 32) {
+      const long long i = base + lane;
+      const double v = i < n ? static_cast<double>(r[i]) : 0.0;
+      const bool fin = i < n && ((static_cast<unsigned long long>(__double_as_longlong(v)) >> 52 & 0x7ff) != 0x7ff);
+      const unsigned m = __ballot_sync(0xffffffffu, fin);
+      if (m) {
+        pv = __shfl_sync(0xffffffffu, v, __ffs(m) - 1);
+        break;
+      }
+    }
+    if (lane == 0) pivots[2 * row + w] = pv;
+  }
+}
+
+template <int OP, typename T>
+__global__ void __launch_bounds__(NT) move_dscan_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                        T* __restrict__ out, long long rows, long long n,
+                                                        long long window, long long min_count,
+                                                        long long tiles_per_row, void* ws_base, size_t ws_bytes,
+                                                        const double* __restrict__ pivots,
+                                                        unsigned* __restrict__ row_flags) {
+  constexpr int NS = Traits<OP>::NS;
+  constexpr bool TWO = Traits<OP>::TWO;
+  constexpr bool VL = Traits<OP>::VARLIKE;
+  typedef typename BitsOf<T>::type B;
+  using S = St<NS>;
+  using dfl::df;
+  // single-input statistics keep each position's difference for the replay
+  constexpr bool CACHE = !TWO;
+  __shared__ B sx[SPAD], so[SPAD];
+  __shared__ B sy[TWO ? SPAD : 1], syo[TWO ? SPAD : 1];
+  __shared__ df sdl[CACHE ? NS : 1][CACHE ? SPAD : 1];
+  __shared__ signed char sdc[CACHE ? SPAD : 1];
+  __shared__ S wtot[NT / 32];
+  __shared__ S carry_smem;
+  __shared__ long long tile_smem;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  Workspace ws = make_workspace(ws_base, ws_bytes);
+  const unsigned epoch = *reinterpret_cast<volatile unsigned*>(&ws.hdr->epoch);
+  const long long total_tiles = rows * tiles_per_row;
+  const unsigned long long last_use = l2_evict_first();
+
+  for (;;) {
+    if (tid == 0) tile_smem = claim_tile(ws.hdr);
+    __syncthreads();
+    const long long tile = tile_smem;
+    if (tile >= total_tiles) break;
+    const TileCoord tc = tile_coord(tile, rows);
+    const long long row = tc.row, chunk = tc.chunk;
+    const long long t0 = chunk * TILE;
+    const B* ar = as_bits(a) + row * n;
+    const B* br = TWO ? as_bits(b) + row * n : nullptr;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      const long long i = t0 + p;
+      const bool in = i < n, old = in && i >= window;
+      sx[spad(p)] = in ? ar[i] : nanb;
+      so[spad(p)] = old ? ld_hint(ar + (i - window), last_use) : nanb;
+      if (TWO) {
+        sy[spad(p)] = in ? br[i] : nanb;
+        syo[spad(p)] = old ? ld_hint(br + (i - window), last_use) : nanb;
+      }
+    }
+    __syncthreads();
+    const double px = VL ? pivots[2 * row] : 0.0;
+    const double py = (VL && TWO) ? pivots[2 * row + 1] : 0.0;
+    const int q0 = tid * KT;
+    bool ok = true;
+    // position k's difference: the entering contributions minus the leaving ones
+    auto delta = [&](int k, df* d, int& dc) {
+      const int sp = spad(q0 + k);
+      const B xi = sx[sp], xo = so[sp];
+      const B yi = TWO ? sy[sp] : xi, yo = TWO ? syo[sp] : xo;
+      df c[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) d[j] = df{0.0f, 0.0f};
+      dc = 0;
+      if (!nan_bits(xi) && !(TWO && nan_bits(yi))) {
+        contrib<OP>(xi, yi, px, py, c, ok);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) d[j] = c[j];
+        dc = 1;
+      }
+      if (!nan_bits(xo) && !(TWO && nan_bits(yo))) {
+        contrib<OP>(xo, yo, px, py, c, ok);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) d[j] = dfl::df_add_fast(d[j], dfl::df_neg(c[j]));
+        --dc;
+      }
+    };
+    // ---- this thread's run of differences, then the warp scan ----
+    S run = st_zero<NS>();
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      df d[NS];
+      int dc;
+      delta(k, d, dc);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) run.s[j] = dfl::df_add_fast(run.s[j], d[j]);
+      run.cnt += dc;
+      if (CACHE) {
+        const int sp = spad(q0 + k);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) sdl[j][sp] = d[j];
+        sdc[sp] = static_cast<signed char>(dc);
+      }
+    }
+    S incl = run;
+#pragma unroll
+    for (int dl = 1; dl < 32; dl <<= 1) {
+      const S up = st_shfl_up(incl, dl);
+      if (lane >= dl) incl = st_add(up, incl);
+    }
+    S e = st_shfl_up(incl, 1);
+    if (lane == 0) e = st_zero<NS>();
+    if (lane == 31) wtot[warp] = incl;
+    __syncthreads();
+    {
+      S w = st_zero<NS>();
+      for (int u = 0; u < warp; ++u) w = st_add(w, wtot[u]);
+      e = st_add(w, e);
+    }
+    // ---- the tile's total, the chained look-back, the carry ----
+    if (tid == 0) {
+      S agg = wtot[0];
+      for (int u = 1; u < NT / 32; ++u) agg = st_add(agg, wtot[u]);
+      S excl = st_zero<NS>();
+      if (chunk > 0) {
+        const long long pred = tile - rows;
+        if (wait_status(ws, pred, epoch) == kStatePrefix) excl = read_payload<S>(ws, pred, kStatePrefix);
+        else record_error(ws.hdr, kLookbackTimeout, static_cast<unsigned>(tile));
+      }
+      if (chunk + 1 < tiles_per_row) publish(ws, tile, epoch, kStatePrefix, st_add(excl, agg));
+      carry_smem = excl;
+    }
+    __syncthreads();
+    // ---- replay from the state entering this thread's run ----
+    S st = st_add(carry_smem, e);
+    T res[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      df d[NS];
+      int dc;
+      if (CACHE) {
+        const int sp = spad(q0 + k);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) d[j] = sdl[j][sp];
+        dc = sdc[sp];
+      } else {
+        delta(k, d, dc);
+      }
+#pragma unroll
+      for (int j = 0; j < NS; ++j) st.s[j] = dfl::df_add_fast(st.s[j], d[j]);
+      st.cnt += dc;
+      res[k] = static_cast<T>(finalize_d<OP>(st, min_count));
+    }
+    const int bad = __syncthreads_or(ok ? 0 : 1);  // every thread has also read its run
+#pragma unroll
+    for (int k = 0; k < KT; ++k)
+      sx[spad(q0 + k)] = sizeof(T) == 8 ? static_cast<B>(__double_as_longlong(static_cast<double>(res[k])))
+                                        : static_cast<B>(__float_as_uint(static_cast<float>(res[k])));
+    __syncthreads();
+    B* ob = as_bits(out) + row * n;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      if (t0 + p < n) ob[t0 + p] = sx[spad(p)];
+    }
+    if (bad && tid == 0) atomicOr(row_flags + row, 1u);
+    __syncthreads();  // the stage is reused by the next tile
+  }
+  if (tid == 0) finish_cta(ws.hdr);
+}
+}  // namespace dsc
 
 // ---------------------------------------------------------------------------------
 // Along a non-last axis: one thread per column
@@ -724,17 +1073,28 @@ using namespace nbg::moving;
 
 namespace {
 
-size_t move_scratch_bytes(long long rows, long long) {
-  return 256 + static_cast<size_t>(kRcpEntries + 1) * 8 + 256 + static_cast<size_t>(rows) * 8 + 256 +
-         static_cast<size_t>(rows + 1) * 8;
+long long dsc_tiles_per_row(long long n) { return n <= 0 ? 0 : (n + dsc::TILE - 1) / dsc::TILE; }
+
+// the exact kernels' tables, then (rows x n calls) the double-float scan's look-back
+// workspace, pivots and row flags
+size_t move_scratch_bytes(long long rows, long long n) {
+  size_t b = 256 + static_cast<size_t>(kRcpEntries + 1) * 8 + 256 + static_cast<size_t>(rows) * 8 + 256 +
+             static_cast<size_t>(rows + 1) * 8;
+  if (n > 0) b += 256 + workspace_bytes(rows * dsc_tiles_per_row(n)) + 256 + static_cast<size_t>(rows) * 16 + 256 +
+                  static_cast<size_t>(rows) * 4;
+  return b;
 }
 
 struct MoveScratch {
   double* rcp;
   long long* first_bad;
   long long* item_start;
+  void* lb;  // look-back workspace of the double-float scan
+  size_t lb_bytes;
+  double* pivots;
+  unsigned* flags;
 };
-MoveScratch carve_move(void* ws, long long rows) {
+MoveScratch carve_move(void* ws, long long rows, long long n = 0) {
   auto up = [](size_t p) { return (p + 255) & ~static_cast<size_t>(255); };
   MoveScratch m;
   size_t p = up(reinterpret_cast<size_t>(ws));
@@ -743,6 +1103,13 @@ MoveScratch carve_move(void* ws, long long rows) {
   m.first_bad = reinterpret_cast<long long*>(p);
   p = up(p + static_cast<size_t>(rows) * 8);
   m.item_start = reinterpret_cast<long long*>(p);
+  p = up(p + static_cast<size_t>(rows + 1) * 8);
+  m.lb = reinterpret_cast<void*>(p);
+  m.lb_bytes = n > 0 ? workspace_bytes(rows * dsc_tiles_per_row(n)) : 0;
+  p = up(p + m.lb_bytes);
+  m.pivots = reinterpret_cast<double*>(p);
+  p = up(p + static_cast<size_t>(rows) * 16);
+  m.flags = reinterpret_cast<unsigned*>(p);
   return m;
 }
 
@@ -763,6 +1130,32 @@ long long chunk_len_for(long long rows, long long n, long long window) {
   return len;
 }
 
+// the double-float scan over rows x n (pivots first for the variance-like statistics)
+template <int OP, typename T>
+int launch_dscan(const T* a, const T* b, T* out, long long rows, long long n, long long window, long long min_count,
+                 const MoveScratch& sc, cudaStream_t stream) {
+  const long long tpr = dsc_tiles_per_row(n);
+  const long long tiles = rows * tpr;
+  if (cudaMemsetAsync(sc.lb, 0, 256 + static_cast<size_t>(tiles) * 8, stream) != cudaSuccess) return kLaunchError;
+  if (Traits<OP>::VARLIKE)
+    dsc::dsc_pivot_kernel<T><<<static_cast<int>((rows * 32 + 255) / 256), 256, 0, stream>>>(
+        a, Traits<OP>::TWO ? b : nullptr, rows, n, sc.pivots);
+  static int per_sm = 0;  // resident CTAs per SM, from the occupancy calculator
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (per_sm == 0) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, dsc::move_dscan_kernel<OP, T>, dsc::NT, 0);
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const long long cap = static_cast<long long>(sms) * per_sm;
+  const int grid = static_cast<int>(tiles < cap ? tiles : cap);
+  dsc::move_dscan_kernel<OP, T><<<grid, dsc::NT, 0, stream>>>(a, b, out, rows, n, window, min_count, tpr, sc.lb,
+                                                              sc.lb_bytes, sc.pivots, sc.flags);
+  return kOk;
+}
+
 // offsets == nullptr: rows x n; else ragged series (n unused), chunk_len 0 = default
 template <int OP, typename T, bool C>
 int launch_move(const T* a, const T* b, T* out, const long long* offsets, long long rows, long long n,
@@ -771,8 +1164,11 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   if (rows < 0 || n < 0 || window <= 0 || min_count < 0 || chunk_len < 0) return kInvalidArgument;
   if (rows == 0 || (!offsets && n == 0)) return kOk;
   if (!a || !out || (Traits<OP>::TWO && !b)) return kInvalidArgument;
-  if (!ws || ws_bytes < move_scratch_bytes(rows, n)) return kWorkspaceTooSmall;
-  const MoveScratch sc = carve_move(ws, rows);
+  // the compensated form over rows runs the double-float scan first (float64 arrays)
+  constexpr bool kDsc = C && sizeof(T) == 8;
+  const bool dsc = kDsc && !offsets;
+  if (!ws || ws_bytes < move_scratch_bytes(rows, dsc ? n : 0)) return kWorkspaceTooSmall;
+  const MoveScratch sc = carve_move(ws, rows, dsc ? n : 0);
   const long long rcp_n = std::min<long long>(window, kRcpEntries);
   Layout lay{offsets, sc.item_start, rows, n, 0};
   long long len;
@@ -790,7 +1186,14 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   }
   const long long setup_items = std::max(rcp_n + 1, rows);
   move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
-      sc.rcp, rcp_n, sc.first_bad, rows);
+      sc.rcp, rcp_n, sc.first_bad, rows, dsc ? sc.flags : nullptr);
+  if constexpr (kDsc) {
+    if (dsc) {
+      const int r = launch_dscan<OP, T>(a, b, out, rows, n, window, min_count, sc, stream);
+      if (r != kOk) return r;
+      launches += Traits<OP>::VARLIKE ? 2 : 1;
+    }
+  }
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
   auto kern = move_kernel<OP, T, C>;
   // the shared-memory opt-in is per device, so it is set on every call
@@ -802,8 +1205,9 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, NT, smem) != cudaSuccess || r < 1) r = 2;
     return r;
   }();
+  // after the double-float scan this recomputes only the rows it flagged
   kern<<<layout_grid(grid_items, per_sm), NT, smem, stream>>>(a, b, out, lay, window, min_count, len, sc.rcp, rcp_n,
-                                                              sc.first_bad);
+                                                              sc.first_bad, dsc ? sc.flags : nullptr);
   move_poison_kernel<T, Traits<OP>::VARLIKE><<<static_cast<int>(std::min<long long>(rows, 4096)), 256, 0, stream>>>(
       out, lay, window, sc.first_bad);
   note_launches(launches);

@@ -97,29 +97,6 @@ struct F64 {
   static NBG_DEVICE T fma(T a, T b, T c) { return ::fma(a, b, c); }
 };
 
-NBG_DEVICE dfl::df df_from_f64(double x) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned sign = static_cast<unsigned>(b >> 63) << 31;
-  const int e = static_cast<int>((b >> 52) & 0x7ff);
-  const unsigned long long m = b & 0x000fffffffffffffull;
-  if (e == 0x7ff) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u | (m ? 0x400000u : 0u))), 0.0f};
-  const int E = e - 1023;
-  if (e == 0 || E < -126) {  // below float32's normal range: a float32 rounding of it
-    const float h = __double2float_rn(x);
-    return dfl::df{h, __double2float_rn(x - static_cast<double>(h))};
-  }
-  if (E > 127) return dfl::df{__int_as_float(static_cast<int>(sign | 0x7f800000u)), 0.0f};
-  const unsigned long long M = m | 0x0010000000000000ull;
-  const float hi = __int_as_float(static_cast<int>(sign | (static_cast<unsigned>(E + 127) << 23) |
-                                                  static_cast<unsigned>((M >> 29) & 0x7fffffu)));
-  const unsigned rem = static_cast<unsigned>(M & ((1ull << 29) - 1));
-  float lo = 0.0f;
-  if (rem && E - 52 >= -126) {
-    lo = __fmul_rn(__uint2float_rn(rem), dfl::pow2f(E - 52));
-    if (sign) lo = -lo;
-  }
-  return dfl::fast_two_sum(hi, lo);
-}
 
 NBG_DEVICE double df_to_f64(dfl::df x) {
   const unsigned hb = static_cast<unsigned>(__float_as_int(x.hi));
@@ -780,11 +757,11 @@ NBG_DEVICE dfl::df df_div_fast(dfl::df x, dfl::df y) {
   const df e = df_sub(x, df_mul_f(y, q1));
   return fast_two_sum(q1, __fmul_rn(e.hi, r));
 }
-// hi + lo in float64 (two conversions and an add on the FP64 pipe, which this form
-// leaves idle) instead of the integer renormalisation of df_to_f64
+// hi + lo in float64: two widenings from the bit patterns and one float64 add (cheaper
+// than the integer renormalisation of df_to_f64)
 NBG_DEVICE double df_out(dfl::df x) {
   if (!isfinite(x.hi)) return static_cast<double>(x.hi);
-  return static_cast<double>(x.hi) + static_cast<double>(x.lo);
+  return df_to_double(x);
 }
 template <int OP>
 NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw) {

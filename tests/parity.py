@@ -141,13 +141,19 @@ def move_scale(name, a, b, window, axis=-1):
         std = oracle.move("move_std", np.asarray(a, dtype=np.float64), window=window, min_count=2, axis=axis)
         with np.errstate(invalid="ignore", divide="ignore"):
             return np.fmax(np.sqrt(sq), sq / std)
-    absb = np.abs(np.asarray(b, dtype=np.float64))
+    # the pair statistics see only the positions where both inputs are valid
+    v = _valid(a, b)
+    a_p = np.where(v, np.asarray(a, dtype=np.float64), np.nan)
+    b_p = np.where(v, np.asarray(b, dtype=np.float64), np.nan)
+    absa, absb = np.abs(a_p), np.abs(b_p)
+    cnt = oracle.move("move_sum", v.astype(np.float64), window=window, min_count=0, axis=axis)
+    sq = oracle.move("move_sum", absa * absa, window=w2, min_count=0, axis=axis) / np.maximum(cnt - 1, 1)
     sqb = oracle.move("move_sum", absb * absb, window=w2, min_count=0, axis=axis) / np.maximum(cnt - 1, 1)
     if name == "move_cov":
         return np.sqrt(sq * sqb)
     # move_corr
-    va = oracle.move("move_var", np.asarray(a, dtype=np.float64), window=window, min_count=2, axis=axis)
-    vb = oracle.move("move_var", np.asarray(b, dtype=np.float64), window=window, min_count=2, axis=axis)
+    va = oracle.move("move_var", a_p, window=window, min_count=2, axis=axis)
+    vb = oracle.move("move_var", b_p, window=window, min_count=2, axis=axis)
     return np.fmax(1.0, np.fmax(_cond(sq, va), _cond(sqb, vb)))
 
 

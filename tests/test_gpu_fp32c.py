@@ -95,3 +95,31 @@ def test_fp32c_deterministic_and_causal():
         part = fn(np.ascontiguousarray(a[:, :150_000]), precision="fp32c", **kw)
         np.testing.assert_array_equal(full, again)
         np.testing.assert_array_equal(full[:, :150_000], part)
+
+
+@pytest.mark.parametrize("fname", MOVE)
+def test_move_fp32c_rows_outside_the_double_float_range(fname):
+    # rows holding an infinity, huge or tiny values are recomputed from exact window sums:
+    # the reference's NaN / infinity placement, and the stated bound elsewhere.  (With an
+    # infinity inside the window numbagg's move_cov gives +-inf or NaN depending on the
+    # signs of the other sums; the exact kernel gives NaN there, a known difference.)
+    a, b = _inputs("normal", (6, 20_000), 34)
+    if fname != "move_cov":  # see the note on infinities in move_cov below
+        a[1, 100] = np.inf
+        a[2, 5000] = -np.inf
+    a[3] *= 1e60
+    a[4] *= 1e-40
+    y = b if fname in TWO else None
+    args = (a, b) if y is not None else (a,)
+    for window in (5, 400):
+        got = getattr(nb, fname)(*args, window=window, min_count=2, precision="fp32c")
+        want = oracle.move(fname, a, y, window=window, min_count=2)
+        ext = oracle.move(fname, a, y, window=window, min_count=2, ext=True)
+        allow = move_degenerate(fname, a, y, window)
+        allow = np.zeros(a.shape, bool) if allow is None else allow
+        assert np.array_equal(np.isnan(got) & ~allow, np.isnan(want) & ~allow), (fname, window)
+        inf = np.isinf(want) & ~allow
+        assert np.array_equal(got[inf], want[inf]), (fname, window)
+        fin = np.isfinite(ext) & np.isfinite(want) & ~allow
+        r = scaled_error(np.where(fin, got, 0.0), np.where(fin, ext, 0.0), move_scale(fname, a, y, window))
+        assert r["max_err"] <= FP32C_TOL, (fname, window, r)
