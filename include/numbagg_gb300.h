@@ -89,8 +89,12 @@ NBG_DECL_MOVE2(move_cov, float, f32)
 NBG_DECL_MOVE2(move_corr, double, f64)
 NBG_DECL_MOVE2(move_corr, float, f32)
 /* FP32-compensated forms of the float64 entry points (no reference counterpart: numbagg
- * computes in float64 only).  The same exact window sums, finalised from exact integer
- * numerators in double-float on the FP32 pipes; about 2^-46 relative error. */
+ * computes in float64 only).  A one-pass double-float window scan on the FP32 pipes
+ * (values minus the row's first finite value for the variance-like statistics); rows
+ * holding an infinity or values beyond its range are recomputed from exact window sums
+ * finalised in double-float.  Stated bound: 2e-6 relative to the window's magnitude;
+ * ws must then be nbg_move_workspace_bytes(rows, n) bytes (it holds the scan's
+ * look-back state). */
 NBG_DECL_MOVE1(move_sum, double, f64_fp32c)
 NBG_DECL_MOVE1(move_mean, double, f64_fp32c)
 NBG_DECL_MOVE1(move_var, double, f64_fp32c)
@@ -122,8 +126,12 @@ NBG_DECL_MOVE_COLS_ALL(float, f32)
  * functions array by array; these run many series of uneven length in one call).
  * values: the series back to back, series s = values[offsets[s] : offsets[s + 1]];
  * offsets: nseries + 1 device int64, offsets[0] = 0, nondecreasing; out: like values.
- * ws: nbg_move_workspace_bytes(nseries, 0) bytes of scratch; chunk_len: positions per
- * work item (0 = default: eight windows, at least 32768). */
+ * ws: scratch of nbg_move_ragged_workspace_bytes(nseries, total) bytes (total: values
+ * in all), with which the _fp32c forms run their double-float tile scan;
+ * nbg_move_workspace_bytes(nseries, 0) bytes suffice for the exact kernels alone.
+ * chunk_len: positions per work item of the exact kernels (0 = default: eight windows,
+ * at least 32768). */
+NBG_API size_t nbg_move_ragged_workspace_bytes(long long nseries, long long total);
 #define NBG_DECL_MOVE_RAGGED(NAME, SFX)                                                          \
   NBG_API int nbg_##NAME##_ragged_##SFX(const double* values, const long long* offsets, long long nseries, \
                                         double* out, long long window, long long min_count,             \

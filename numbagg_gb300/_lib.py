@@ -94,6 +94,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         sig(f"nbg_{f}_f64_fp32c", c_i, c_vp, c_vp, c_vp, c_d, c_i, c_d, c_vp, c_ll, c_ll, c_vp, c_sz, c_vp)
     # ragged batches
     sig("nbg_move_exp_ragged_workspace_bytes", c_sz, c_ll, c_ll)
+    sig("nbg_move_ragged_workspace_bytes", c_sz, c_ll, c_ll)
     sig("nbg_group_ragged_workspace_bytes", c_sz, c_ll, c_ll, c_ll)
     for sfx in ("f64", "f64_fp32c"):
         for f in ("move_sum", "move_mean", "move_var", "move_std"):

@@ -733,15 +733,17 @@ NBG_DEVICE double finalize_d(const St<Traits<OP>::NS>& st, long long min_count) 
   return df_out(df_div(nab, df_sqrt(vv)));
 }
 
-// the row's pivot: its first finite value (0 when it has none)
+// the row's (or ragged series') pivot: its first finite value (0 when it has none)
 template <typename T>
 __global__ void dsc_pivot_kernel(const T* __restrict__ a, const T* __restrict__ b, long long rows, long long n,
-                                 double* __restrict__ pivots) {
+                                 const long long* __restrict__ offsets, double* __restrict__ pivots) {
   const int lane = threadIdx.x & 31;
   const long long row = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   if (row >= rows) return;
+  if (offsets) n = offsets[row + 1] - offsets[row];
+  const long long base = offsets ? offsets[row] : row * n;
   for (int w = 0; w < (b ? 2 : 1); ++w) {
-    const T* r = (w ? b : a) + row * n;
+    const T* r = (w ? b : a) + base;
     double pv = 0.0;
     for (long long base = 0; base < n; base += 32) {
       const long long i = base + lane;
@@ -917,6 +919,148 @@ __global__ void __launch_bounds__(NT) move_dscan_kernel(const T* __restrict__ a,
     __syncthreads();  // the stage is reused by the next tile
   }
   if (tid == 0) finish_cta(ws.hdr);
+}
+
+// Ragged series (single-input statistics): three phases, since a chained scan would
+// serialise the tiles of a long series.  Phase 0 folds each tile's differences into its
+// total (aggs[tile]); dsc_carry_kernel scans every series' totals in order; phase 2
+// replays each tile from carries[tile].  Tiles beyond the workspace's capacity flag their
+// series for the exact kernel.
+template <int OP, typename T, int PHASE>
+__global__ void __launch_bounds__(NT) move_dtile_kernel(const T* __restrict__ a, T* __restrict__ out, Layout lay,
+                                                        long long window, long long min_count,
+                                                        St<Traits<OP>::NS>* __restrict__ aggs,
+                                                        const St<Traits<OP>::NS>* __restrict__ carries,
+                                                        long long capacity, const double* __restrict__ pivots,
+                                                        unsigned* __restrict__ row_flags) {
+  constexpr int NS = Traits<OP>::NS;
+  constexpr bool VL = Traits<OP>::VARLIKE;
+  static_assert(!Traits<OP>::TWO, "single-input statistics");
+  typedef typename BitsOf<T>::type B;
+  using S = St<NS>;
+  using dfl::df;
+  __shared__ B sx[SPAD], so[SPAD];
+  __shared__ df sdl[NS][SPAD];
+  __shared__ signed char sdc[SPAD];
+  __shared__ S wtot[NT / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const B nanb = sizeof(B) == 8 ? static_cast<B>(0x7ff8000000000000ull) : static_cast<B>(0x7fc00000u);
+  const long long items = layout_items(lay);
+  const unsigned long long last_use = l2_evict_first();
+  for (long long id = blockIdx.x; id < items; id += gridDim.x) {
+    const Item it = layout_item(lay, id);
+    const long long row = it.row, n = it.len;
+    if (id >= capacity) {  // beyond the workspace: the exact kernel takes the series
+      if (PHASE == 0 && tid == 0) atomicOr(row_flags + row, 1u);
+      continue;
+    }
+    const long long t0 = it.index * TILE;
+    const B* ar = as_bits(a) + it.base;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      const long long i = t0 + p;
+      const bool in = i < n, old = in && i >= window;
+      sx[spad(p)] = in ? ar[i] : nanb;
+      so[spad(p)] = old ? ld_hint(ar + (i - window), last_use) : nanb;
+    }
+    __syncthreads();
+    const double px = VL ? pivots[2 * row] : 0.0;
+    const int q0 = tid * KT;
+    bool ok = true;
+    S run = st_zero<NS>();
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      const int sp = spad(q0 + k);
+      const B xi = sx[sp], xo = so[sp];
+      df c[NS], d[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) d[j] = df{0.0f, 0.0f};
+      int dc = 0;
+      if (!nan_bits(xi)) {
+        contrib<OP>(xi, xi, px, px, c, ok);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) d[j] = c[j];
+        dc = 1;
+      }
+      if (!nan_bits(xo)) {
+        contrib<OP>(xo, xo, px, px, c, ok);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) d[j] = dfl::df_add_fast(d[j], dfl::df_neg(c[j]));
+        --dc;
+      }
+#pragma unroll
+      for (int j = 0; j < NS; ++j) run.s[j] = dfl::df_add_fast(run.s[j], d[j]);
+      run.cnt += dc;
+      if (PHASE == 2) {
+#pragma unroll
+        for (int j = 0; j < NS; ++j) sdl[j][sp] = d[j];
+        sdc[sp] = static_cast<signed char>(dc);
+      }
+    }
+    S incl = run;
+#pragma unroll
+    for (int dl = 1; dl < 32; dl <<= 1) {
+      const S up = st_shfl_up(incl, dl);
+      if (lane >= dl) incl = st_add(up, incl);
+    }
+    S e = st_shfl_up(incl, 1);
+    if (lane == 0) e = st_zero<NS>();
+    if (lane == 31) wtot[warp] = incl;
+    const int bad = __syncthreads_or(ok ? 0 : 1);
+    if (PHASE == 0) {
+      if (tid == 0) {
+        S agg = wtot[0];
+        for (int u = 1; u < NT / 32; ++u) agg = st_add(agg, wtot[u]);
+        aggs[id] = agg;
+        if (bad) atomicOr(row_flags + row, 1u);
+      }
+      __syncthreads();  // the stage is reused by the next tile
+      continue;
+    }
+    {
+      S w = carries[id];
+      for (int u = 0; u < warp; ++u) w = st_add(w, wtot[u]);
+      e = st_add(w, e);
+    }
+    S st = e;
+    T res[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      const int sp = spad(q0 + k);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) st.s[j] = dfl::df_add_fast(st.s[j], sdl[j][sp]);
+      st.cnt += sdc[sp];
+      res[k] = static_cast<T>(finalize_d<OP>(st, min_count));
+    }
+    __syncthreads();  // every thread has read its run
+#pragma unroll
+    for (int k = 0; k < KT; ++k)
+      sx[spad(q0 + k)] = static_cast<B>(__double_as_longlong(static_cast<double>(res[k])));
+    __syncthreads();
+    B* ob = as_bits(out) + it.base;
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      const int p = j * NT + tid;
+      if (t0 + p < n) ob[t0 + p] = sx[spad(p)];
+    }
+    __syncthreads();
+  }
+}
+
+// per series, the state entering each tile: its earlier tiles' totals added in order
+template <int NS>
+__global__ void dsc_carry_kernel(const St<NS>* __restrict__ aggs, St<NS>* __restrict__ carries,
+                                 const long long* __restrict__ item_start, long long nseries, long long capacity) {
+  const long long srs = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (srs >= nseries) return;
+  const long long first = item_start[srs];
+  const long long last = item_start[srs + 1] < capacity ? item_start[srs + 1] : capacity;
+  St<NS> run = st_zero<NS>();
+  for (long long t = first; t < last; ++t) {
+    carries[t] = run;
+    run = st_add(run, aggs[t]);
+  }
 }
 }  // namespace dsc
 
@@ -1130,6 +1274,51 @@ long long chunk_len_for(long long rows, long long n, long long window) {
   return len;
 }
 
+// Ragged series: the exact kernels' scratch, then pivots, flags, the tile plan and the
+// double-float tile totals and carries (single-input statistics: at most two sums).
+constexpr size_t kDscRaggedTileBytes = 2 * sizeof(dsc::St<2>);
+size_t dsc_ragged_fixed_bytes(long long nseries) {
+  return move_scratch_bytes(nseries, 0) + 256 + static_cast<size_t>(nseries) * 16 + 256 +
+         static_cast<size_t>(nseries) * 4 + 256 + static_cast<size_t>(nseries + 1) * 8 + 256;
+}
+size_t move_ragged_scratch_bytes(long long nseries, long long total) {
+  const long long tiles = total / dsc::TILE + nseries;
+  return dsc_ragged_fixed_bytes(nseries) + static_cast<size_t>(tiles) * kDscRaggedTileBytes;
+}
+
+template <int OP, typename T>
+int launch_dtile(const T* a, T* out, const long long* offsets, long long nseries, long long window,
+                 long long min_count, const MoveScratch& sc, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  using S = dsc::St<Traits<OP>::NS>;
+  auto up = [](size_t p) { return (p + 255) & ~static_cast<size_t>(255); };
+  size_t p = up(reinterpret_cast<size_t>(sc.flags) + static_cast<size_t>(nseries) * 4);
+  long long* tile_start = reinterpret_cast<long long*>(p);
+  p = up(p + static_cast<size_t>(nseries + 1) * 8);
+  const size_t end = reinterpret_cast<size_t>(ws) + ws_bytes;
+  const long long capacity = end > p ? static_cast<long long>((end - p) / (2 * sizeof(S))) : 0;
+  S* aggs = reinterpret_cast<S*>(p);
+  S* carries = aggs + capacity;
+  ragged_plan_kernel<<<1, 1024, 0, stream>>>(offsets, nseries, dsc::TILE, tile_start);
+  if (Traits<OP>::VARLIKE)
+    dsc::dsc_pivot_kernel<T><<<static_cast<int>((nseries * 32 + 255) / 256), 256, 0, stream>>>(a, nullptr, nseries, 0,
+                                                                                             offsets, sc.pivots);
+  Layout lay{offsets, tile_start, nseries, 0, 0};
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, dsc::move_dtile_kernel<OP, T, 2>, dsc::NT, 0);
+    per_sm = nb > 0 ? nb : 1;
+  }
+  const int grid = layout_grid(LLONG_MAX, per_sm);
+  dsc::move_dtile_kernel<OP, T, 0><<<grid, dsc::NT, 0, stream>>>(a, out, lay, window, min_count, aggs, carries,
+                                                                  capacity, sc.pivots, sc.flags);
+  dsc::dsc_carry_kernel<Traits<OP>::NS><<<static_cast<int>((nseries + 255) / 256), 256, 0, stream>>>(
+      aggs, carries, tile_start, nseries, capacity);
+  dsc::move_dtile_kernel<OP, T, 2><<<grid, dsc::NT, 0, stream>>>(a, out, lay, window, min_count, aggs, carries,
+                                                                  capacity, sc.pivots, sc.flags);
+  return (Traits<OP>::VARLIKE ? 5 : 4);
+}
+
 // the double-float scan over rows x n (pivots first for the variance-like statistics)
 template <int OP, typename T>
 int launch_dscan(const T* a, const T* b, T* out, long long rows, long long n, long long window, long long min_count,
@@ -1139,7 +1328,7 @@ int launch_dscan(const T* a, const T* b, T* out, long long rows, long long n, lo
   if (cudaMemsetAsync(sc.lb, 0, 256 + static_cast<size_t>(tiles) * 8, stream) != cudaSuccess) return kLaunchError;
   if (Traits<OP>::VARLIKE)
     dsc::dsc_pivot_kernel<T><<<static_cast<int>((rows * 32 + 255) / 256), 256, 0, stream>>>(
-        a, Traits<OP>::TWO ? b : nullptr, rows, n, sc.pivots);
+        a, Traits<OP>::TWO ? b : nullptr, rows, n, nullptr, sc.pivots);
   static int per_sm = 0;  // resident CTAs per SM, from the occupancy calculator
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
@@ -1166,9 +1355,12 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   if (!a || !out || (Traits<OP>::TWO && !b)) return kInvalidArgument;
   // the compensated form over rows runs the double-float scan first (float64 arrays)
   constexpr bool kDsc = C && sizeof(T) == 8;
-  const bool dsc = kDsc && !offsets;
-  if (!ws || ws_bytes < move_scratch_bytes(rows, dsc ? n : 0)) return kWorkspaceTooSmall;
-  const MoveScratch sc = carve_move(ws, rows, dsc ? n : 0);
+  // ragged single-input series take the three-phase double-float scan when the scratch
+  // holds its tile plan (nbg_move_ragged_workspace_bytes), else the exact kernel alone
+  const bool dtile = kDsc && offsets && !Traits<OP>::TWO && ws_bytes >= dsc_ragged_fixed_bytes(rows) + kDscRaggedTileBytes;
+  const bool dsc = (kDsc && !offsets) || dtile;
+  if (!ws || ws_bytes < move_scratch_bytes(rows, (kDsc && !offsets) ? n : 0)) return kWorkspaceTooSmall;
+  const MoveScratch sc = carve_move(ws, rows, (kDsc && !offsets) ? n : 0);
   const long long rcp_n = std::min<long long>(window, kRcpEntries);
   Layout lay{offsets, sc.item_start, rows, n, 0};
   long long len;
@@ -1188,10 +1380,13 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
       sc.rcp, rcp_n, sc.first_bad, rows, dsc ? sc.flags : nullptr);
   if constexpr (kDsc) {
-    if (dsc) {
+    if (dsc && !offsets) {
       const int r = launch_dscan<OP, T>(a, b, out, rows, n, window, min_count, sc, stream);
       if (r != kOk) return r;
       launches += Traits<OP>::VARLIKE ? 2 : 1;
+    } else if (dtile) {
+      if constexpr (!Traits<OP>::TWO) launches += launch_dtile<OP, T>(a, out, offsets, rows, window, min_count, sc, ws,
+                                                                      ws_bytes, stream);
     }
   }
   const size_t smem = static_cast<size_t>(Traits<OP>::TWO ? 4 : 2) * SPAD * sizeof(typename BitsOf<T>::type);
@@ -1231,6 +1426,9 @@ int launch_move_cols(const T* a, const T* b, T* out, long long outer, long long 
 extern "C" {
 
 size_t nbg_move_workspace_bytes(long long rows, long long n) { return move_scratch_bytes(rows, n); }
+size_t nbg_move_ragged_workspace_bytes(long long nseries, long long total) {
+  return nseries < 0 || total < 0 ? 0 : move_ragged_scratch_bytes(nseries, total);
+}
 
 #define NBG_MOVE1(NAME, OPC, T, SFX, C)                                                        \
   int nbg_##NAME##_##SFX(const T* a, T* out, long long rows, long long n, long long window,  \

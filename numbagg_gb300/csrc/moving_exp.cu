@@ -331,6 +331,9 @@ constexpr int TILE = NT * KT;
 constexpr int SPAD = TILE + TILE / KT;
 NBG_DEVICE int spad(int p) { return p + p / KT; }
 
+template <int OP>
+NBG_DEVICE double finalize_dfast(const dfl::df* s, int seen, dfl::df mw);
+
 // Phase 0 (PHASE == 0): the map of each tile, composed in position order, to maps[].
 // Phase 2 (PHASE == 2): outputs, starting from the state carries[tile] before the tile.
 // One CTA per tile; tiles do not wait on each other.
@@ -383,6 +386,7 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
   const V al_s = as_num(N(), alpha_scalar);
   const V d_s = N::sub(N::one(), al_s);
   const V dd_s = N::mul(d_s, d_s);
+  const dfl::df mw_df = df_from_f64(min_weight);
   const int q0 = tid * KT;
 
   auto position = [&](int k, V& x, V& y, V& al, V& d, V& dd, bool& valid, bool& in) {
@@ -475,7 +479,11 @@ __global__ void __launch_bounds__(NT) exp_tile_kernel(const T* __restrict__ a, c
       for (int j = 0; j < NS; ++j) s[j] = N::add(s[j], bj[j]);
       seen = 1;
     }
-    const T rt = static_cast<T>(finalize<OP>(N(), s, seen, min_weight));
+    // the double-float form finalises like the one-pass scan (divisions cleared)
+    double r;
+    if constexpr (N::kDF) r = finalize_dfast<OP>(s, seen, mw_df);
+    else r = finalize<OP>(N(), s, seen, min_weight);
+    const T rt = static_cast<T>(r);
     sx[spad(q0 + k)] = sizeof(T) == 8 ? static_cast<B>(__double_as_longlong(static_cast<double>(rt)))
                                       : static_cast<B>(__float_as_uint(static_cast<float>(rt)));
   }

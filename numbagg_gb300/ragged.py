@@ -74,7 +74,7 @@ def _move(name, values, offsets, window, min_count, precision, chunk_len, out=No
     out = torch.empty_like(values) if out is None else out
     if nseries and values.numel():
         L = _lib.lib()
-        ws = _lib.workspaces.scratch(L.nbg_move_workspace_bytes(nseries, 0), values.device)
+        ws = _lib.workspaces.scratch(L.nbg_move_ragged_workspace_bytes(nseries, values.numel()), values.device)
         fn = getattr(L, f"nbg_{name}_ragged_{_sfx(precision)}")
         _lib.check(
             fn(values.data_ptr(), offsets.data_ptr(), nseries, out.data_ptr(), window, min_count, int(chunk_len or 0),

@@ -1,9 +1,9 @@
 """The FP32-compensated ("fp32c") forms against the extended-precision oracle.
 
 ``precision="fp32c"`` (an extension of numbagg's signatures) computes the float64
-moving-window and exponentially weighted functions on the FP32 pipes: exact window
-sums finalised in double-float, and the EWM scan in double-float with the
-shift-invariant statistics taken on pivoted values.  The stated bound is a relative
+moving-window and exponentially weighted functions on the FP32 pipes: double-float
+window sums and a double-float EWM scan, the shift-invariant statistics taken on
+pivoted values; rows outside the double-float range fall back to exact window sums.  The stated bound is a relative
 error of at most 2e-6 against a well-conditioned float64 oracle, here the long-double
 restatement of numbagg's loops (oracle ``ext=True``), on ordinary data and on the
 precision-stress data 1e6 + N(0, 1) with correlation 0.7 and 2% NaN.  Errors are
