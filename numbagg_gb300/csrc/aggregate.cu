@@ -23,16 +23,15 @@ constexpr int AT = 256;
 constexpr long long kNone = LLONG_MAX;  // no column selected yet
 
 struct Part {
-  fx::i128 fx;             // float sums, half the elements: exact fixed-point sum of the
-                           // values (or, in the variance's second pass, of the squared
-                           // deviations)
-  double s;                // the other half, summed in float64
+  fx::i128 fx;             // float sums, half the elements: exact fixed-point sum
+  double s;                // the other half, summed in float64 (and the variance's
+                           // squared deviations)
   long long i;             // integer sum, wrapping like the reference's integer loops
   long long cnt;           // elements that are not NaN
   unsigned long long key;  // selection: order key of the best element
   long long idx;           // and its column (kNone: none)
-  int sc;                  // fx's scale: the largest biased exponent met (twice it for squares)
-  int pinf, ninf, bad;     // +inf / -inf terms, NaN terms (a NaN deviation)
+  int sc;                  // fx's scale: the largest biased exponent met
+  int pinf, ninf;          // +inf / -inf terms of a float sum
 };
 
 NBG_DEVICE Part none_part() {
@@ -44,7 +43,7 @@ NBG_DEVICE Part none_part() {
   p.key = 0ull;
   p.idx = kNone;
   p.sc = 0;
-  p.pinf = p.ninf = p.bad = 0;
+  p.pinf = p.ninf = 0;
   return p;
 }
 
@@ -63,7 +62,6 @@ NBG_DEVICE Part combine(const Part& a, const Part& b) {
   r.idx = take_b ? b.idx : a.idx;
   r.pinf = a.pinf + b.pinf;
   r.ninf = a.ninf + b.ninf;
-  r.bad = a.bad + b.bad;
   return r;
 }
 
@@ -81,7 +79,6 @@ NBG_DEVICE Part shfl_part(const Part& v, int o) {
   r.sc = __shfl_xor_sync(0xffffffffu, v.sc, o);
   r.pinf = __shfl_xor_sync(0xffffffffu, v.pinf, o);
   r.ninf = __shfl_xor_sync(0xffffffffu, v.ninf, o);
-  r.bad = __shfl_xor_sync(0xffffffffu, v.bad, o);
   return r;
 }
 
@@ -94,13 +91,8 @@ NBG_DEVICE double part_sum(const Part& r) {
   if (r.ninf > 0) return __longlong_as_double(static_cast<long long>(0xfff0000000000000ull));
   return fx::to_f64(r.fx, fx::lsb_value(r.sc)) + r.s;
 }
-// the squared deviations (sc is twice the scale exponent): NaN if a deviation was
-// NaN, inf if one overflowed
-NBG_DEVICE double part_ssq(const Part& r) {
-  if (r.bad > 0) return quiet_nan(0.0);
-  if (r.pinf > 0) return __longlong_as_double(0x7ff0000000000000ll);
-  return fx::to_f64(r.fx, fx::lsb_product(r.sc / 2, r.sc / 2)) + r.s;
-}
+// the squared deviations (summed in float64)
+NBG_DEVICE double part_ssq(const Part& r) { return r.s; }
 
 // order keys: x < y  <=>  key(x) < key(y) for non-NaN values, -0.0 == +0.0
 NBG_DEVICE unsigned long long sel_key(double x) { return order_key_ieee(x); }
@@ -144,18 +136,11 @@ NBG_DEVICE void absorb(Part& p, T x, long long c, double mu) {
   if (is_nan(x)) return;
   ++p.cnt;
   if (DEV) {
-    // (x - mean)^2 summed (numbagg/funcs.py:120-126), the deviation rounded like the
-    // reference's
+    // (x - mean)^2 summed in float64 (numbagg/funcs.py:120-126): an infinite or NaN
+    // deviation carries into the sum as in the reference; an exact fixed-point square
+    // costs more integer work than it saves
     const double d = static_cast<double>(x) - mu;
-    if (is_nan(d)) {
-      ++p.bad;
-      return;
-    }
-    if (fx::is_inf(d)) {
-      ++p.pinf;
-      return;
-    }
-    p.s = fma(d, d, p.s);  // the exact square costs more integer work than it saves
+    p.s = fma(d, d, p.s);
   } else if (F == kSum || F == kMean || F == kVar || F == kStd) {
     if (IsFloat<T>::value) {
       const double xd = static_cast<double>(x);
@@ -199,8 +184,9 @@ __global__ void __launch_bounds__(AT) agg_part_kernel(const T* __restrict__ a, l
   Part p = none_part();
   // float sums: four loads in flight per thread before any of them is consumed (a
   // loop-carried sum would otherwise leave one load per thread outstanding, too few to
-  // cover DRAM latency); the other statistics keep the plain loop, which measured faster
-  constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value;
+  // cover DRAM latency); the other statistics and the variance's second pass keep the
+  // plain loop, which measured faster for them
+  constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value && !DEV;
   long long c = c0 + threadIdx.x;
   if (!SUM) {
     for (; c < c1; c += AT) absorb<F, T, DEV, false>(p, ar[c], c, mu);
@@ -253,7 +239,7 @@ __global__ void __launch_bounds__(AT) agg_cols_part_kernel(const T* __restrict__
     const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
     const double mu = DEV ? mean[col] : 0.0;
     constexpr int W = AT / 32;
-    constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value;
+    constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value && !DEV;
     long long r = c0 + warp;
     if (!SUM) {
 #pragma unroll 4
