@@ -711,7 +711,9 @@ NBG_DEVICE double finalize_d(const St<Traits<OP>::NS>& st, long long min_count) 
   using namespace dfl;
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
   const long long c = st.cnt;
-  if (OP == kSum) return c >= min_count ? df_out(st.s[0]) : nan;
+  // an empty window sums to exactly zero (the double-float prefix differences would
+  // leave the rounding residue of the values that came and went)
+  if (OP == kSum) return c >= min_count ? (c == 0 ? 0.0 : df_out(st.s[0])) : nan;
   if (OP == kMean) return c >= (min_count > 1 ? min_count : 1) ? df_out(df_div_count(st.s[0], c)) : nan;
   const df cd = df_of_count(c);
   if (OP == kVar || OP == kStd || OP == kCov) {

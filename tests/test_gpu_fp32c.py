@@ -123,3 +123,23 @@ def test_move_fp32c_rows_outside_the_double_float_range(fname):
         fin = np.isfinite(ext) & np.isfinite(want) & ~allow
         r = scaled_error(np.where(fin, got, 0.0), np.where(fin, ext, 0.0), move_scale(fname, a, y, window))
         assert r["max_err"] <= FP32C_TOL, (fname, window, r)
+
+
+@pytest.mark.parametrize("fname", MOVE)
+def test_move_fp32c_edges(fname):
+    # tile edges of the double-float scan (1024 positions), a single row, all-NaN rows,
+    # windows of 1 and of the whole row, min_count 0
+    rng = np.random.default_rng(35)
+    for rows, n in ((1, 1), (1, 1025), (3, 3073), (2, 5000)):
+        a = rng.standard_normal((rows, n))
+        b = 0.5 * a + rng.standard_normal((rows, n))
+        a[rng.random(a.shape) < 0.2] = np.nan
+        if rows > 1:
+            a[1] = np.nan
+        y = b if fname in TWO else None
+        args = (a, b) if y is not None else (a,)
+        for window, mc in ((1, 0), (1, 1), (min(7, n), 2), (n, 1)):
+            got = getattr(nb, fname)(*args, window=window, min_count=mc, precision="fp32c")
+            ext = oracle.move(fname, a, y, window=window, min_count=mc, ext=True)
+            r = scaled_error(got, ext, move_scale(fname, a, y, window), move_degenerate(fname, a, y, window))
+            assert r["nan_mismatch"] == 0 and r["max_err"] <= FP32C_TOL, (fname, rows, n, window, mc, r)
