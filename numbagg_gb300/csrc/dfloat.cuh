@@ -303,6 +303,7 @@ NBG_DEVICE double widen_f32(float x) {
 NBG_DEVICE double df_to_double(dfl::df x) { return widen_f32(x.hi) + widen_f32(x.lo); }
 // a nonnegative count below 2^31 as a double-float, exactly
 NBG_DEVICE dfl::df df_of_int(long long c) {
+  if (c < (1ll << 24)) return dfl::df{f32_of_count(c), 0.0f};
   const int ci = static_cast<int>(c);
   const float hi = __int2float_rn(ci);
   return dfl::df{hi, __int2float_rn(ci - __float2int_rz(hi))};

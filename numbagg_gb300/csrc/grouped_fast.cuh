@@ -531,7 +531,7 @@ NBG_DEVICE double div_by_count(double s, long long c, const double* __restrict__
   if (c > kRcpN || !finite) return s / static_cast<double>(c);
   const double r = __ldg(rcp + c);
   const double q0 = s * r;
-  const double e = fma(-q0, static_cast<double>(c), s);
+  const double e = fma(-q0, f64_of_count(c), s);
   return fma(e, r, q0);
 }
 

@@ -258,7 +258,7 @@ NBG_DEVICE double rcp_of(long long c, const double* __restrict__ rcp, long long 
 NBG_DEVICE double div_count(double s, long long c, double r) {
   if (!finite_bits(s)) return s / static_cast<double>(c);
   const double q0 = s * r;
-  const double e = fma(-q0, static_cast<double>(c), s);
+  const double e = fma(-q0, f64_of_count(c), s);
   return fma(e, r, q0);
 }
 
@@ -645,17 +645,59 @@ NBG_DEVICE bool raw_ok(unsigned long long b) {
   return (b << 1) == 0 || (e >= 1023 - 100 && e <= 1023 + 100);
 }
 // a pivoted value zero or at least 2^-60 in magnitude
-NBG_DEVICE bool piv_ok(double y) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(y));
-  return (b << 1) == 0 || static_cast<int>((b >> 52) & 0x7ff) >= 1023 - 60;
+NBG_DEVICE bool piv_ok(dfl::df y) {
+  const unsigned b = __float_as_uint(y.hi);
+  return (b << 1) == 0u || static_cast<int>((b >> 23) & 0xff) >= 127 - 60;
+}
+
+// The pivot as a signed integer mantissa and biased exponent, and x - p from the two
+// integer mantissas aligned at the larger exponent (9 guard bits, so the difference is
+// exact whenever the exponents are within 9 and within 2^-53 of |x - p| otherwise),
+// normalised into a double-float (48 bits) with integer instructions: no float64
+// subtraction on the FP64 pipe.
+struct Piv {
+  long long m;
+  int e;
+  double d;  // the pivot itself
+};
+NBG_DEVICE Piv piv_of(double p) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(p));
+  const int e0 = static_cast<int>((b >> 52) & 0x7ff);
+  long long m = static_cast<long long>((b & 0x000fffffffffffffull) | (e0 ? 0x0010000000000000ull : 0ull));
+  if (b >> 63) m = -m;
+  return Piv{m, e0 ? e0 : 1, p};
+}
+NBG_DEVICE dfl::df sub_pivot(unsigned long long xb, Piv p) {
+  const int e0 = static_cast<int>((xb >> 52) & 0x7ff);
+  const int ex = e0 ? e0 : 1;
+  long long mx = static_cast<long long>((xb & 0x000fffffffffffffull) | (e0 ? 0x0010000000000000ull : 0ull));
+  if (xb >> 63) mx = -mx;
+  const int E = ex > p.e ? ex : p.e;
+  const int sx = E - ex, sp = E - p.e;
+  const long long X = sx > 61 ? (mx < 0 ? -1ll : 0ll) : (mx * 512) >> sx;  // |mx * 512| < 2^62
+  const long long P = sp > 61 ? (p.m < 0 ? -1ll : 0ll) : (p.m * 512) >> sp;
+  const long long D = X - P;  // |D| < 2^63
+  if (D == 0) return dfl::df{0.0f, 0.0f};
+  const unsigned sign = D < 0 ? 0x80000000u : 0u;
+  const unsigned long long U = static_cast<unsigned long long>(D < 0 ? -D : D);
+  const int lz = __clzll(static_cast<long long>(U));
+  const unsigned long long N = U << lz;  // leading one at bit 63
+  const int fe = E - 894 - lz;           // float32 exponent field of the leading one
+  if (fe < 1 + 48 || fe > 254)  // outside float32's comfortable range: the general path
+    return df_from_f64(__longlong_as_double(static_cast<long long>(xb)) - p.d);
+  const float hi = __uint_as_float(sign | (static_cast<unsigned>(fe) << 23) | static_cast<unsigned>((N >> 40) & 0x7fffffu));
+  const unsigned L = static_cast<unsigned>((N >> 16) & 0xffffffu);  // the next 24 bits (the rest truncated)
+  float l = __fmul_rn(__uint2float_rn(L), __uint_as_float(static_cast<unsigned>(fe - 47) << 23));
+  if (sign) l = -l;
+  return dfl::df{hi, l};
 }
 
 // One position's contributions (the value pair is valid): x for sums and means; the
-// pivoted y = x - p (one float64 subtraction, exact for values near the pivot), y^2
+// pivoted y = x - p (sub_pivot), y^2
 // (variance); ya, yb, ya yb (covariance); + ya^2, yb^2 (correlation).  `ok` turns
 // false when a value is outside the range above.
 template <int OP>
-NBG_DEVICE void contrib(unsigned long long xb, unsigned long long yb, double px, double py, dfl::df* c, bool& ok) {
+NBG_DEVICE void contrib(unsigned long long xb, unsigned long long yb, Piv px, Piv py, dfl::df* c, bool& ok) {
   constexpr bool VL = Traits<OP>::VARLIKE, TWO = Traits<OP>::TWO;
   using namespace dfl;
   ok = ok && raw_ok<VL>(xb) && (!TWO || raw_ok<VL>(yb));
@@ -663,17 +705,17 @@ NBG_DEVICE void contrib(unsigned long long xb, unsigned long long yb, double px,
     c[0] = df_from_f64(__longlong_as_double(static_cast<long long>(xb)));
     return;
   }
-  const double xd = __longlong_as_double(static_cast<long long>(xb)) - px;
-  ok = ok && piv_ok(xd);
-  const df x = df_from_f64(xd);
+  // one input: the float64 subtraction (its pipe has room here); two inputs: the
+  // integer one (measured faster for each)
+  const df x = TWO ? sub_pivot(xb, px) : df_from_f64(__longlong_as_double(static_cast<long long>(xb)) - px.d);
+  ok = ok && piv_ok(x);
   if (OP == kVar || OP == kStd) {
     c[0] = x;
     c[1] = df_mul(x, x);
     return;
   }
-  const double yd = __longlong_as_double(static_cast<long long>(yb)) - py;
-  ok = ok && piv_ok(yd);
-  const df y = df_from_f64(yd);
+  const df y = sub_pivot(yb, py);
+  ok = ok && piv_ok(y);
   c[0] = x;
   c[1] = y;
   c[2] = df_mul(x, y);
@@ -686,11 +728,12 @@ NBG_DEVICE void contrib(unsigned long long xb, unsigned long long yb, double px,
 // s / c for a count c >= 1 (exact in float32 below 2^24)
 NBG_DEVICE dfl::df df_div_count(dfl::df s, long long c) {
   using namespace dfl;
-  const float cf = static_cast<float>(c);
-  if (c < (1ll << 24)) {
-    const float q1 = __fdiv_rn(s.hi, cf);
+  const float cf = f32_of_count(c);
+  if (c < (1ll << 24)) {  // a reciprocal, a quotient and one corrected quotient (~2^-44)
+    const float rc = __frcp_rn(cf);
+    const float q1 = __fmul_rn(s.hi, rc);
     const df r = df_sub(s, two_prod(q1, cf));
-    return fast_two_sum(q1, __fdiv_rn(r.hi, cf));
+    return fast_two_sum(q1, __fmul_rn(r.hi, rc));
   }
   const double cd = static_cast<double>(c);
   return df_div(s, df_from_f64(cd));
@@ -813,8 +856,8 @@ __global__ void __launch_bounds__(NT) move_dscan_kernel(const T* __restrict__ a,
       }
     }
     __syncthreads();
-    const double px = VL ? pivots[2 * row] : 0.0;
-    const double py = (VL && TWO) ? pivots[2 * row + 1] : 0.0;
+    const Piv px = piv_of(VL ? pivots[2 * row] : 0.0);
+    const Piv py = piv_of((VL && TWO) ? pivots[2 * row + 1] : 0.0);
     const int q0 = tid * KT;
     bool ok = true;
     // position k's difference: the entering contributions minus the leaving ones
@@ -967,7 +1010,7 @@ __global__ void __launch_bounds__(NT) move_dtile_kernel(const T* __restrict__ a,
       so[spad(p)] = old ? ld_hint(ar + (i - window), last_use) : nanb;
     }
     __syncthreads();
-    const double px = VL ? pivots[2 * row] : 0.0;
+    const Piv px = piv_of(VL ? pivots[2 * row] : 0.0);
     const int q0 = tid * KT;
     bool ok = true;
     S run = st_zero<NS>();

@@ -144,6 +144,23 @@ NBG_DEVICE unsigned ld_hint(const unsigned* a, unsigned long long pol) {
 // the quiet NaN numpy writes (np.nan), in the type of the argument
 NBG_DEVICE double quiet_nan(double) { return __longlong_as_double(0x7ff8000000000000ll); }
 NBG_DEVICE float quiet_nan(float) { return __int_as_float(0x7fc00000); }
+// Counts as floating-point values built from their bit patterns: the conversion
+// instructions from 64-bit integers execute on this GPU's slow FP64 pipe.
+// Exact for 0 <= c < 2^53 (float64) and 0 <= c < 2^24 (float32).
+NBG_DEVICE double f64_of_count(long long c) {
+  if (c <= 0) return c == 0 ? 0.0 : static_cast<double>(c);
+  const int lz = __clzll(c);
+  const unsigned long long frac = ((static_cast<unsigned long long>(c) << lz) << 1) >> 12;
+  return __longlong_as_double(static_cast<long long>((static_cast<unsigned long long>(1086 - lz) << 52) | frac));
+}
+NBG_DEVICE float f32_of_count(long long c) {
+  if (c <= 0 || c >= (1ll << 24)) return static_cast<float>(c);
+  const unsigned u = static_cast<unsigned>(c);
+  const int lz = __clz(static_cast<int>(u));
+  const unsigned frac = ((u << lz) << 1) >> 9;
+  return __uint_as_float((static_cast<unsigned>(158 - lz) << 23) | frac);
+}
+
 NBG_DEVICE bool is_nan(double x) {
   const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
   return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
