@@ -11,7 +11,7 @@
 // from them.  Float sums take half their elements in an exact 128-bit fixed-point sum
 // and half in float64 (numba accumulates in float64, or in float32 for the float32
 // nansum); every reduction order is fixed, so results are the same run to run.
-#include "fixed128.cuh"
+#include "dfloat.cuh"
 
 #include <climits>
 
@@ -25,7 +25,8 @@ constexpr long long kNone = LLONG_MAX;  // no column selected yet
 struct Part {
   fx::i128 fx;             // float sums, half the elements: exact fixed-point sum
   double s;                // the other half, summed in float64 (and the variance's
-                           // squared deviations)
+                           // squared deviations outside the double-float range)
+  dfl::df q;               // the variance's squared deviations, in double-float
   long long i;             // integer sum, wrapping like the reference's integer loops
   long long cnt;           // elements that are not NaN
   unsigned long long key;  // selection: order key of the best element
@@ -38,6 +39,7 @@ NBG_DEVICE Part none_part() {
   Part p;
   p.fx = 0;
   p.s = 0.0;
+  p.q = dfl::df{0.0f, 0.0f};
   p.i = 0;
   p.cnt = 0;
   p.key = 0ull;
@@ -55,6 +57,7 @@ NBG_DEVICE Part combine(const Part& a, const Part& b) {
   r.sc = a.sc > b.sc ? a.sc : b.sc;
   r.fx = fx::shr(a.fx, r.sc - a.sc) + fx::shr(b.fx, r.sc - b.sc);
   r.s = a.s + b.s;
+  r.q = dfl::df_add(a.q, b.q);
   r.i = static_cast<long long>(static_cast<unsigned long long>(a.i) + static_cast<unsigned long long>(b.i));
   r.cnt = a.cnt + b.cnt;
   const bool take_b = b.idx != kNone && (a.idx == kNone || b.key > a.key || (b.key == a.key && b.idx < a.idx));
@@ -72,6 +75,7 @@ NBG_DEVICE Part shfl_part(const Part& v, int o) {
   r.fx = static_cast<fx::i128>((static_cast<fx::u128>(__shfl_xor_sync(0xffffffffu, hi, o)) << 64) |
                                __shfl_xor_sync(0xffffffffu, lo, o));
   r.s = __shfl_xor_sync(0xffffffffu, v.s, o);
+  r.q = dfl::df{__shfl_xor_sync(0xffffffffu, v.q.hi, o), __shfl_xor_sync(0xffffffffu, v.q.lo, o)};
   r.i = __shfl_xor_sync(0xffffffffu, v.i, o);
   r.cnt = __shfl_xor_sync(0xffffffffu, v.cnt, o);
   r.key = __shfl_xor_sync(0xffffffffu, v.key, o);
@@ -91,8 +95,10 @@ NBG_DEVICE double part_sum(const Part& r) {
   if (r.ninf > 0) return __longlong_as_double(static_cast<long long>(0xfff0000000000000ull));
   return fx::to_f64(r.fx, fx::lsb_value(r.sc)) + r.s;
 }
-// the squared deviations (summed in float64)
-NBG_DEVICE double part_ssq(const Part& r) { return r.s; }
+// the squared deviations: the double-float sum and the float64 one
+NBG_DEVICE double part_ssq(const Part& r) {
+  return (static_cast<double>(r.q.hi) + static_cast<double>(r.q.lo)) + r.s;
+}
 
 // order keys: x < y  <=>  key(x) < key(y) for non-NaN values, -0.0 == +0.0
 NBG_DEVICE unsigned long long sel_key(double x) { return order_key_ieee(x); }
@@ -136,11 +142,18 @@ NBG_DEVICE void absorb(Part& p, T x, long long c, double mu) {
   if (is_nan(x)) return;
   ++p.cnt;
   if (DEV) {
-    // (x - mean)^2 summed in float64 (numbagg/funcs.py:120-126): an infinite or NaN
-    // deviation carries into the sum as in the reference; an exact fixed-point square
-    // costs more integer work than it saves
+    // (x - mean)^2 summed (numbagg/funcs.py:120-126): the deviation rounded in float64
+    // as the reference's, its square and the sum in double-float on the FP32 pipes
+    // (about 2^-46 relative, and the squares are all positive, so nothing cancels);
+    // deviations whose square leaves float32's range, infinities and NaN take float64
     const double d = static_cast<double>(x) - mu;
-    p.s = fma(d, d, p.s);
+    const int ed = static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(d)) >> 52) & 0x7ff);
+    if (ed >= 1023 - 60 && ed <= 1023 + 60) {
+      const dfl::df dd = df_from_f64(d);
+      p.q = dfl::df_add_fast(p.q, dfl::df_mul(dd, dd));
+    } else {
+      p.s = fma(d, d, p.s);
+    }
   } else if (F == kSum || F == kMean || F == kVar || F == kStd) {
     if (IsFloat<T>::value) {
       const double xd = static_cast<double>(x);
@@ -184,9 +197,8 @@ __global__ void __launch_bounds__(AT) agg_part_kernel(const T* __restrict__ a, l
   Part p = none_part();
   // float sums: four loads in flight per thread before any of them is consumed (a
   // loop-carried sum would otherwise leave one load per thread outstanding, too few to
-  // cover DRAM latency); the other statistics and the variance's second pass keep the
-  // plain loop, which measured faster for them
-  constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value && !DEV;
+  // cover DRAM latency); the other statistics keep the plain loop, which measured faster
+  constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value;
   long long c = c0 + threadIdx.x;
   if (!SUM) {
     for (; c < c1; c += AT) absorb<F, T, DEV, false>(p, ar[c], c, mu);
@@ -239,7 +251,7 @@ __global__ void __launch_bounds__(AT) agg_cols_part_kernel(const T* __restrict__
     const long long c0 = chunk * chunk_len, c1 = min(m, c0 + chunk_len);
     const double mu = DEV ? mean[col] : 0.0;
     constexpr int W = AT / 32;
-    constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value && !DEV;
+    constexpr bool SUM = (F == kSum || F == kMean || F == kVar || F == kStd) && IsFloat<T>::value;
     long long r = c0 + warp;
     if (!SUM) {
 #pragma unroll 4
