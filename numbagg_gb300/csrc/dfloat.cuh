@@ -309,4 +309,46 @@ NBG_DEVICE dfl::df df_of_int(long long c) {
   return dfl::df{hi, __int2float_rn(ci - __float2int_rz(hi))};
 }
 
+// The pivot as a signed integer mantissa and biased exponent, and x - p from the two
+// integer mantissas aligned at the larger exponent (9 guard bits, so the difference is
+// exact whenever the exponents are within 9 and within 2^-53 of |x - p| otherwise),
+// normalised into a double-float (48 bits) with integer instructions: no float64
+// subtraction on the FP64 pipe.
+struct Piv {
+  long long m;
+  int e;
+  double d;  // the pivot itself
+};
+NBG_DEVICE Piv piv_of(double p) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(p));
+  const int e0 = static_cast<int>((b >> 52) & 0x7ff);
+  long long m = static_cast<long long>((b & 0x000fffffffffffffull) | (e0 ? 0x0010000000000000ull : 0ull));
+  if (b >> 63) m = -m;
+  return Piv{m, e0 ? e0 : 1, p};
+}
+NBG_DEVICE dfl::df sub_pivot(unsigned long long xb, Piv p) {
+  const int e0 = static_cast<int>((xb >> 52) & 0x7ff);
+  const int ex = e0 ? e0 : 1;
+  long long mx = static_cast<long long>((xb & 0x000fffffffffffffull) | (e0 ? 0x0010000000000000ull : 0ull));
+  if (xb >> 63) mx = -mx;
+  const int E = ex > p.e ? ex : p.e;
+  const int sx = E - ex, sp = E - p.e;
+  const long long X = sx > 61 ? (mx < 0 ? -1ll : 0ll) : (mx * 512) >> sx;  // |mx * 512| < 2^62
+  const long long P = sp > 61 ? (p.m < 0 ? -1ll : 0ll) : (p.m * 512) >> sp;
+  const long long D = X - P;  // |D| < 2^63
+  if (D == 0) return dfl::df{0.0f, 0.0f};
+  const unsigned sign = D < 0 ? 0x80000000u : 0u;
+  const unsigned long long U = static_cast<unsigned long long>(D < 0 ? -D : D);
+  const int lz = __clzll(static_cast<long long>(U));
+  const unsigned long long N = U << lz;  // leading one at bit 63
+  const int fe = E - 894 - lz;           // float32 exponent field of the leading one
+  if (fe < 1 + 48 || fe > 254)  // outside float32's comfortable range: the general path
+    return df_from_f64(__longlong_as_double(static_cast<long long>(xb)) - p.d);
+  const float hi = __uint_as_float(sign | (static_cast<unsigned>(fe) << 23) | static_cast<unsigned>((N >> 40) & 0x7fffffu));
+  const unsigned L = static_cast<unsigned>((N >> 16) & 0xffffffu);  // the next 24 bits (the rest truncated)
+  float l = __fmul_rn(__uint2float_rn(L), __uint_as_float(static_cast<unsigned>(fe - 47) << 23));
+  if (sign) l = -l;
+  return dfl::df{hi, l};
+}
+
 }  // namespace nbg

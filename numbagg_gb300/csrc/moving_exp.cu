@@ -116,7 +116,9 @@ struct DF {
   static NBG_DEVICE T mul(T a, T b) { return dfl::df_mul(a, b); }
   static NBG_DEVICE T add(T a, T b) { return dfl::df_add(a, b); }
   static NBG_DEVICE T sub(T a, T b) { return dfl::df_sub(a, b); }
-  static NBG_DEVICE T fma(T a, T b, T c) { return dfl::df_add(dfl::df_mul(a, b), c); }
+  // the decayed recurrences' multiply-add: the product plus the cheaper sum (about
+  // 2^-44 of the terms' magnitudes, far inside the compensated form's bound)
+  static NBG_DEVICE T fma(T a, T b, T c) { return dfl::df_add_fast(dfl::df_mul(a, b), c); }
 };
 
 // a value of the array as the policy's number (float64 policy: exact widening)
@@ -625,19 +627,6 @@ NBG_DEVICE double fdiv(double a, double b) {
   const double q0 = a * r;
   return fma(fma(-q0, b, a), r, q0);
 }
-// a / b nearly correctly rounded (Markstein's sequence: the float32 reciprocal refined
-// once, then the quotient corrected once; P. Markstein, IBM J. Res. Dev. 34(1), 1990):
-// for the quotients that feed a cancellation (the bias 1 - sw2 / sw^2 and the biased
-// variance), whose errors the subtraction amplifies
-NBG_DEVICE double mdiv(double a, double b) {
-  const unsigned eb = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(b)) >> 52) & 0x7ffu;
-  const unsigned ea = static_cast<unsigned>(static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7ffu;
-  if (eb < 1023 - 120 || eb > 1023 + 120 || ea == 0x7ffu) return a / b;
-  double r = rcp_seed(b);
-  r = fma(fma(-b, r, 1.0), r, r);
-  const double q0 = a * r;
-  return fma(fma(-q0, b, a), r, q0);
-}
 
 // x >= y for float64 values on the integer pipes (false if either is NaN): the
 // comparisons of the finalisation, which the FP64 pipe would otherwise execute
@@ -689,8 +678,9 @@ NBG_DEVICE double rcp2(double b) {
 // the divisions cleared: var = (sw sum_x2 - sum_x^2) / (sw^2 - sw2) is var_biased / bias
 // multiplied through by sw^2, cov the same, and the correlation's three centred sums
 // take one reciprocal of sw.  Every cancellation keeps the reference's conditioning
-// (the same differences of the same products), the one quotient is taken nearly
-// correctly rounded (mdiv), and the NaN decisions are the reference's (bias_positive,
+// (the same differences of the same products) and happens before the one quotient,
+// which is therefore not amplified and is taken to about 2^-46 (fdiv); the NaN
+// decisions are the reference's (bias_positive,
 // weight >= min_weight, the denominator > 0).  Exponents outside the ranges those forms
 // assume take the reference's expressions with IEEE divisions.
 template <int OP>
@@ -733,14 +723,14 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
     const double num = fma(s[0], s[2], -(s[1] * s[1]));
     const unsigned en = exp_bits(num);
     if (en == 0x7ffu || en > 1023 + 900) return finalize_ref<OP>(s, min_weight);
-    const double v = mdiv(num, d);
+    const double v = fdiv(num, d);
     return OP == kStd ? sqrt(v) : v;
   }
   if (OP == kCov) {
     const double num = fma(s[2], s[3], -(s[0] * s[1]));
     const unsigned en = exp_bits(num);
     if (en == 0x7ffu || en > 1023 + 900) return finalize_ref<OP>(s, min_weight);
-    return mdiv(num, d);
+    return fdiv(num, d);
   }
   // kCorr
   const double r = rcp2(s[3]);
@@ -748,7 +738,7 @@ NBG_DEVICE double finalize_fast(const double* s, int seen, double min_weight) {
   const double v1 = fma(-(s[0] * s[0]), r, s[6]);
   const double v2 = fma(-(s[1] * s[1]), r, s[7]);
   const double den = sqrt(v1 * v2);
-  return gt0_f64(den) ? mdiv(cov, den) : nan;
+  return gt0_f64(den) ? fdiv(cov, den) : nan;
 }
 
 // Double-float finalisation of the one-pass scan: min_weight converted once per
