@@ -145,10 +145,11 @@ NBG_DEVICE void absorb(Part& p, T x, long long c, double mu) {
     // (x - mean)^2 summed (numbagg/funcs.py:120-126): the deviation rounded in float64
     // as the reference's, its square and the sum in double-float on the FP32 pipes
     // (about 2^-46 relative, and the squares are all positive, so nothing cancels);
-    // deviations whose square leaves float32's range, infinities and NaN take float64
+    // deviations beyond 2^(+-40) (whose squares, summed, could leave float32's range),
+    // zeros, infinities and NaN take float64
     const double d = static_cast<double>(x) - mu;
     const int ed = static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(d)) >> 52) & 0x7ff);
-    if (ed >= 1023 - 60 && ed <= 1023 + 60) {
+    if (ed >= 1023 - 40 && ed <= 1023 + 40) {
       const dfl::df dd = df_from_f64(d);
       p.q = dfl::df_add_fast(p.q, dfl::df_mul(dd, dd));
     } else {

@@ -1360,8 +1360,11 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   constexpr bool kDsc = C && sizeof(T) == 8;
   // ragged single-input series take the three-phase double-float scan when the scratch
   // holds its tile plan (nbg_move_ragged_workspace_bytes), else the exact kernel alone
-  const bool dtile = kDsc && offsets && !Traits<OP>::TWO && ws_bytes >= dsc_ragged_fixed_bytes(rows) + kDscRaggedTileBytes;
-  const bool dsc = (kDsc && !offsets) || dtile;
+  // (windows below 2^24 keep the double-float window sums inside float32's range for the
+  // value ranges the scan accepts; longer ones take the exact kernel)
+  const bool dtile = kDsc && offsets && !Traits<OP>::TWO && window < (1ll << 24) &&
+                     ws_bytes >= dsc_ragged_fixed_bytes(rows) + kDscRaggedTileBytes;
+  const bool dsc = (kDsc && !offsets && window < (1ll << 24)) || dtile;
   if (!ws || ws_bytes < move_scratch_bytes(rows, (kDsc && !offsets) ? n : 0)) return kWorkspaceTooSmall;
   const MoveScratch sc = carve_move(ws, rows, (kDsc && !offsets) ? n : 0);
   const long long rcp_n = std::min<long long>(window, kRcpEntries);
@@ -1383,7 +1386,7 @@ int launch_move(const T* a, const T* b, T* out, const long long* offsets, long l
   move_setup_kernel<<<static_cast<int>(std::min<long long>((setup_items + 255) / 256, 1024)), 256, 0, stream>>>(
       sc.rcp, rcp_n, sc.first_bad, rows, dsc ? sc.flags : nullptr);
   if constexpr (kDsc) {
-    if (dsc && !offsets) {
+    if (dsc && !offsets) {  // rows x n
       const int r = launch_dscan<OP, T>(a, b, out, rows, n, window, min_count, sc, stream);
       if (r != kOk) return r;
       launches += Traits<OP>::VARLIKE ? 2 : 1;
