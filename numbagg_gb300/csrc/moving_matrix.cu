@@ -132,13 +132,14 @@ __global__ void __launch_bounds__(NT) matrix_kernel(const T* __restrict__ a, T* 
     si[r] = sj[r] = pr[r] = qi[r] = qj[r] = T(0);
     cnt[r] = 0;
   }
+  const bool whole = i0 + IB <= n_vars;  // every row of the block exists (uniform)
   auto update = [&](long long t, bool add) {
     const T* row = ab + t * n_vars;
     const T vj = row[jj];
     if (is_nan(vj)) return;
 #pragma unroll
     for (int r = 0; r < IB; ++r) {
-      if (i0 + r >= n_vars) break;
+      if (!whole && i0 + r >= n_vars) break;
       const T vi = __ldg(row + i0 + r);
       if (is_nan(vi)) continue;
       if (add) {
@@ -167,11 +168,12 @@ __global__ void __launch_bounds__(NT) matrix_kernel(const T* __restrict__ a, T* 
   for (long long t = t0; t < t1; ++t) {
     if (t >= window) update(t - window, false);
     update(t, true);
+    T* o = ob + (t * n_vars + i0) * n_vars + j;
 #pragma unroll
-    for (int r = 0; r < IB; ++r) {
-      if (i0 + r >= n_vars) break;
+    for (int r = 0; r < IB; ++r, o += n_vars) {
+      if (!whole && i0 + r >= n_vars) break;
       const T res = finish<CORR>(si[r], sj[r], pr[r], qi[r], qj[r], cnt[r], mc, rcp);
-      if (active) __stcs(ob + (t * n_vars + i0 + r) * n_vars + j, res);
+      if (active) __stcs(o, res);
     }
   }
 }
