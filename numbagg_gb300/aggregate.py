@@ -73,6 +73,20 @@ def _axes(axis, ndim: int) -> tuple[int, ...]:
     return out
 
 
+def middle_inner(shape, axes) -> int | None:
+    """The product of the trailing unreduced axes when the reduced axes are consecutive,
+    in increasing order and not last, with at least _MIN_INNER outputs per reduced
+    position: such axes are reduced in place through their stride (numbagg's gufuncs
+    read them so), with no copy.  None otherwise."""
+    if not axes:
+        return None
+    k0 = axes[0]
+    if axes != tuple(range(k0, k0 + len(axes))) or axes[-1] >= len(shape) - 1:
+        return None
+    inner = math.prod(shape[axes[-1] + 1 :])
+    return inner if inner >= _MIN_INNER else None
+
+
 def _aggregate(name: str, arr, axis, *, ddof=None):
     dt = _np_dtype(arr)
     loops = _FLOAT_LOOPS if name in ("nanmean", "nanvar", "nanstd") else _INT_FLOAT_LOOPS
@@ -100,17 +114,8 @@ def _aggregate(name: str, arr, axis, *, ddof=None):
     work = _NP_TO_TORCH[loop]
     if a.dtype != work:
         a = a.to(work)
-    # reduced axes that are consecutive, in increasing order and not last: reduced in
-    # place through their stride (numbagg's gufuncs read them so), no copy
-    k0 = axes[0] if axes else 0
-    inner = math.prod(shape[axes[-1] + 1 :]) if axes else 1
-    middle = (
-        len(axes) > 0
-        and axes == tuple(range(k0, k0 + len(axes)))
-        and axes[-1] < len(shape) - 1
-        and inner >= _MIN_INNER
-        and a.is_contiguous()
-    )
+    inner = middle_inner(shape, axes) if a.is_contiguous() else None
+    middle = inner is not None
     flat = None
     if not middle:
         flat = torch.movedim(a, axes, tuple(range(len(shape) - len(axes), len(shape)))).contiguous().reshape(rows, m)

@@ -127,3 +127,26 @@ def test_bench_cpu_sample_is_a_prefix_of_the_workload():
     np.testing.assert_array_equal(np.asarray(v), values[:, :sc].numpy())
     assert b.sample_bytes(rows, sc) > 0
     assert str(sc) in b.sample_desc(rows, sc)
+
+
+def test_in_place_layouts():
+    import torch
+
+    from numbagg_gb300 import _host
+    from numbagg_gb300.aggregate import middle_inner
+
+    # scans: a non-last axis of a C-contiguous array with enough columns
+    t = torch.empty((100, 4096))
+    assert _host.column_layout(t, 0) == (1, 100, 4096)
+    assert _host.column_layout(t, 1) is None  # the last axis: the rows kernels
+    assert _host.column_layout(torch.empty((3, 50, 1000)), 1) == (3, 50, 1000)
+    assert _host.column_layout(torch.empty((100, 7)), 0) is None  # too few columns
+    assert _host.column_layout(torch.empty((4096, 100)).T, 0) is None  # not contiguous
+    # static aggregations: consecutive middle axes, increasing, not last
+    assert middle_inner((4, 40, 50, 64), (1, 2)) == 64
+    assert middle_inner((4, 40, 50, 64), (0,)) == 40 * 50 * 64
+    assert middle_inner((4, 40, 50, 64), (2, 1)) is None  # order matters for argmax
+    assert middle_inner((4, 40, 50, 64), (1, 3)) is None  # not consecutive
+    assert middle_inner((4, 40, 50, 64), (2, 3)) is None  # includes the last axis
+    assert middle_inner((400, 8), (0,)) is None  # fewer outputs than a warp
+    assert middle_inner((5,), ()) is None
