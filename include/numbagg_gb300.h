@@ -323,6 +323,26 @@ NBG_DECL_GROUP_ALL(nanprod)           /* numbagg/grouped.py:124-132 */
 NBG_DECL_GROUP_ALL(nanany)            /* numbagg/grouped.py:247-257 */
 NBG_DECL_GROUP_ALL(nanall)            /* numbagg/grouped.py:260-270 */
 
+/* Along non-last axes, in place: float64 values whose reduced axes are consecutive and
+ * not last, a C-contiguous (outer, m, inner) array with labels over m (the reduced axes
+ * flattened, numbagg's np.ndindex order); out[(o * inner + i) * K + k].  One thread per
+ * column runs numbagg's loop, so the results are the reference's bit for bit.  No
+ * workspace; K at most nbg_group_cols_max_labels(func) (func: 0 sum, 1 mean, 2 count,
+ * 3 var, 4 std), else NBG_UNSUPPORTED. */
+NBG_API size_t nbg_group_cols_max_labels(int func);
+#define NBG_DECL_GROUP_COLS(NAME)                                                                          \
+  NBG_API int nbg_group_##NAME##_cols_f64_i32(const double* values, const int* labels, double* out,       \
+                                              long long outer, long long m, long long inner, long long K,  \
+                                              long long ddof, void* stream);                               \
+  NBG_API int nbg_group_##NAME##_cols_f64_i64(const double* values, const long long* labels, double* out, \
+                                              long long outer, long long m, long long inner, long long K,  \
+                                              long long ddof, void* stream);
+NBG_DECL_GROUP_COLS(nansum)
+NBG_DECL_GROUP_COLS(nanmean)
+NBG_DECL_GROUP_COLS(nancount)
+NBG_DECL_GROUP_COLS(nanvar)
+NBG_DECL_GROUP_COLS(nanstd)
+
 /* Ragged batches of labelled reductions (no reference counterpart): values and labels
  * flat (`total` values), series s = [offsets[s], offsets[s + 1]) with its own labels;
  * out: nseries x num_labels float64 (num_labels <= 8192).  Deterministic: per-chunk

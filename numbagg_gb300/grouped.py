@@ -105,6 +105,9 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
         work = torch.int64
     else:
         work = v.dtype
+    cols = _group_columns(name, v, lab, moved_axes, num_labels, ddof)
+    if cols is not None:
+        return restore(cols)
     if moved_axes is None:
         core = v.ndim
     else:
@@ -151,6 +154,38 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
     if work != result_dtype:
         res = res.to(result_dtype)
     return restore(res)
+
+
+_COLS_FUNCS = {"nansum": 0, "nanmean": 1, "nancount": 2, "nanvar": 3, "nanstd": 4}
+
+
+def _group_columns(name, v, lab, moved_axes, num_labels, ddof):
+    """float64 values reduced over consecutive, increasing, non-last axes of a
+    C-contiguous array: one thread per column runs numbagg's loop in place (no copy, the
+    reference's sums bit for bit).  None when that does not apply."""
+    if name not in _COLS_FUNCS or v.dtype != torch.float64 or not moved_axes or not v.is_contiguous():
+        return None
+    axes = tuple(moved_axes)
+    k0 = axes[0]
+    if axes != tuple(range(k0, k0 + len(axes))) or axes[-1] >= v.ndim - 1:
+        return None
+    L = _lib.lib()
+    if num_labels > L.nbg_group_cols_max_labels(_COLS_FUNCS[name]):
+        return None
+    outer = math.prod(v.shape[:k0])
+    m = math.prod(v.shape[k0 : axes[-1] + 1])
+    inner = math.prod(v.shape[axes[-1] + 1 :])
+    if outer * inner < _host.MIN_COLUMNS:
+        return None
+    lab_dt = torch.int64 if lab.dtype == torch.int64 else torch.int32
+    flat_lab = lab.to(lab_dt).contiguous().reshape(m)
+    out = torch.empty(tuple(v.shape[:k0]) + tuple(v.shape[axes[-1] + 1 :]) + (num_labels,), dtype=v.dtype,
+                      device=v.device)
+    if out.numel():
+        fn = getattr(L, f"nbg_group_{name}_cols_f64_{'i64' if lab_dt == torch.int64 else 'i32'}")
+        _lib.check(fn(v.data_ptr() if m else None, flat_lab.data_ptr() if m else None, out.data_ptr(), outer, m, inner,
+                      num_labels, int(ddof), _host.stream(v.device)), f"group_{name}")
+    return out
 
 
 def _make(name: str, doc_lines: str):

@@ -160,3 +160,30 @@ def test_flox_style_grouped_calls():
             assert_bit_equal(got, want, f)
         else:
             np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12, err_msg=f)
+
+
+@pytest.mark.parametrize("fname", ["group_nansum", "group_nanmean", "group_nancount", "group_nanvar", "group_nanstd"])
+def test_group_non_last_axes_bit_exact(fname):
+    # float64 values grouped over consecutive leading / middle axes: one thread per column
+    # runs numbagg's loop in place, so the sums are the reference's bit for bit
+    rng = np.random.default_rng(44)
+    cases = [((700, 4096), 0, 12), ((3, 40, 50, 2100), (1, 2), 7), ((5, 300, 2048), 1, 30)]
+    for shape, axis, K in cases:
+        x = rng.standard_normal(shape) * 3 + 1
+        x[rng.random(shape) < 0.1] = np.nan
+        ax = (axis,) if isinstance(axis, int) else axis
+        lshape = tuple(shape[a] for a in ax)
+        labels = rng.integers(-1, K + 2, size=lshape)  # negative and >= num_labels skipped
+        xt = torch.from_numpy(x).cuda()
+        lt = torch.from_numpy(labels).cuda()
+        kw = {"ddof": 0} if fname in ("group_nanvar", "group_nanstd") else {}
+        got = getattr(nb, fname)(xt, lt, axis=axis, num_labels=K, **kw).cpu().numpy()
+        want = oracle.group(fname, x, labels, axis=axis, num_labels=K, **kw)
+        assert got.shape == want.shape, (shape, axis)
+        assert_bit_equal(got, want, f"{fname} {shape} axis={axis}")
+    # more labels than the shared-memory bins hold: the moved-axis path, same values
+    x = rng.standard_normal((200, 2048))
+    labels = rng.integers(0, 3000, size=200)
+    got = getattr(nb, fname)(x, labels, axis=0, num_labels=3000)
+    want = oracle.group(fname, x, labels, axis=0, num_labels=3000)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12, equal_nan=True)
