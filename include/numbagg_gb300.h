@@ -323,25 +323,39 @@ NBG_DECL_GROUP_ALL(nanprod)           /* numbagg/grouped.py:124-132 */
 NBG_DECL_GROUP_ALL(nanany)            /* numbagg/grouped.py:247-257 */
 NBG_DECL_GROUP_ALL(nanall)            /* numbagg/grouped.py:260-270 */
 
-/* Along non-last axes, in place: float64 values whose reduced axes are consecutive and
- * not last, a C-contiguous (outer, m, inner) array with labels over m (the reduced axes
- * flattened, numbagg's np.ndindex order); out[(o * inner + i) * K + k].  One thread per
- * column runs numbagg's loop, so the results are the reference's bit for bit.  No
- * workspace; K at most nbg_group_cols_max_labels(func) (func: 0 sum, 1 mean, 2 count,
- * 3 var, 4 std), else NBG_UNSUPPORTED. */
+/* Along non-last axes, in place: values whose reduced axes are consecutive and not last,
+ * a C-contiguous (outer, m, inner) array with labels over m (the reduced axes flattened,
+ * numbagg's np.ndindex order); out[(o * inner + i) * K + k], in the values dtype like the
+ * row entry points above.  One thread per column runs numbagg's loop, so the results are
+ * the reference's bit for bit.  No workspace; K at most nbg_group_cols_max_labels(func)
+ * (func: 0 sum, 1 mean, 2 count, 3 var, 4 std, 5 sum_of_squares, 6 prod, 7 argmax,
+ * 8 argmin, 9 max, 10 min, 11 first, 12 last, 13 any, 14 all), else NBG_UNSUPPORTED.
+ * nanmean/nanvar/nanstd take float values only (numbagg computes integers in float64). */
 NBG_API size_t nbg_group_cols_max_labels(int func);
-#define NBG_DECL_GROUP_COLS(NAME)                                                                          \
-  NBG_API int nbg_group_##NAME##_cols_f64_i32(const double* values, const int* labels, double* out,       \
-                                              long long outer, long long m, long long inner, long long K,  \
-                                              long long ddof, void* stream);                               \
-  NBG_API int nbg_group_##NAME##_cols_f64_i64(const double* values, const long long* labels, double* out, \
-                                              long long outer, long long m, long long inner, long long K,  \
-                                              long long ddof, void* stream);
-NBG_DECL_GROUP_COLS(nansum)
-NBG_DECL_GROUP_COLS(nanmean)
-NBG_DECL_GROUP_COLS(nancount)
-NBG_DECL_GROUP_COLS(nanvar)
-NBG_DECL_GROUP_COLS(nanstd)
+#define NBG_DECL_GROUP_COLS1(NAME, V, VS, L, LS)                                                 \
+  NBG_API int nbg_group_##NAME##_cols_##VS##_##LS(const V* values, const L* labels, V* out,      \
+                                                  long long outer, long long m, long long inner, \
+                                                  long long K, long long ddof, void* stream);
+#define NBG_DECL_GROUP_COLS_L(NAME, V, VS) \
+  NBG_DECL_GROUP_COLS1(NAME, V, VS, int, i32) NBG_DECL_GROUP_COLS1(NAME, V, VS, long long, i64)
+#define NBG_DECL_GROUP_COLS_FLOAT(NAME) NBG_DECL_GROUP_COLS_L(NAME, double, f64) NBG_DECL_GROUP_COLS_L(NAME, float, f32)
+#define NBG_DECL_GROUP_COLS_ALL(NAME) \
+  NBG_DECL_GROUP_COLS_FLOAT(NAME) NBG_DECL_GROUP_COLS_L(NAME, int, i32) NBG_DECL_GROUP_COLS_L(NAME, long long, i64)
+NBG_DECL_GROUP_COLS_ALL(nansum)
+NBG_DECL_GROUP_COLS_ALL(nancount)
+NBG_DECL_GROUP_COLS_FLOAT(nanmean)
+NBG_DECL_GROUP_COLS_FLOAT(nanvar)
+NBG_DECL_GROUP_COLS_FLOAT(nanstd)
+NBG_DECL_GROUP_COLS_ALL(nansum_of_squares)
+NBG_DECL_GROUP_COLS_ALL(nanprod)
+NBG_DECL_GROUP_COLS_ALL(nanargmax)
+NBG_DECL_GROUP_COLS_ALL(nanargmin)
+NBG_DECL_GROUP_COLS_ALL(nanmax)
+NBG_DECL_GROUP_COLS_ALL(nanmin)
+NBG_DECL_GROUP_COLS_ALL(nanfirst)
+NBG_DECL_GROUP_COLS_ALL(nanlast)
+NBG_DECL_GROUP_COLS_ALL(nanany)
+NBG_DECL_GROUP_COLS_ALL(nanall)
 
 /* Ragged batches of labelled reductions (no reference counterpart): values and labels
  * flat (`total` values), series s = [offsets[s], offsets[s + 1]) with its own labels;

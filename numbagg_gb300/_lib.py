@@ -106,9 +106,10 @@ def _declare(lib: ctypes.CDLL) -> None:
             sig(f"nbg_group_{f}_ragged_f64_{ls}", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_vp, c_sz, c_vp)
     # grouped reductions over non-last axes, in place
     sig("nbg_group_cols_max_labels", c_sz, c_i)
-    for f in ("nansum", "nanmean", "nancount", "nanvar", "nanstd"):
-        for ls in ("i32", "i64"):
-            sig(f"nbg_group_{f}_cols_f64_{ls}", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
+    for f in GROUP_FUNC_IDS:
+        for vs in ("f64", "f32") if f in ("nanmean", "nanvar", "nanstd") else ("f64", "f32", "i32", "i64"):
+            for ls in ("i32", "i64"):
+                sig(f"nbg_group_{f}_cols_{vs}_{ls}", c_i, c_vp, c_vp, c_vp, c_ll, c_ll, c_ll, c_ll, c_ll, c_vp)
     for dt in ("f64", "f32", "i32", "i64"):
         for f in ("ffill", "bfill"):
             sig(f"nbg_{f}_{dt}", c_i, c_vp, c_vp, c_ll, c_ll, c_ll, c_vp, c_sz, c_vp)

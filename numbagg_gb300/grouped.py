@@ -156,21 +156,21 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
     return restore(res)
 
 
-_COLS_FUNCS = {"nansum": 0, "nanmean": 1, "nancount": 2, "nanvar": 3, "nanstd": 4}
+_COLS_DTYPES = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
 
 
 def _group_columns(name, v, lab, moved_axes, num_labels, ddof):
-    """float64 values reduced over consecutive, increasing, non-last axes of a
-    C-contiguous array: one thread per column runs numbagg's loop in place (no copy, the
-    reference's sums bit for bit).  None when that does not apply."""
-    if name not in _COLS_FUNCS or v.dtype != torch.float64 or not moved_axes or not v.is_contiguous():
+    """Values reduced over consecutive, increasing, non-last axes of a C-contiguous
+    array: one thread per column runs numbagg's loop in place (no copy, the reference's
+    results bit for bit).  None when that does not apply."""
+    if v.dtype not in _COLS_DTYPES or not moved_axes or not v.is_contiguous():
         return None
     axes = tuple(moved_axes)
     k0 = axes[0]
     if axes != tuple(range(k0, k0 + len(axes))) or axes[-1] >= v.ndim - 1:
         return None
     L = _lib.lib()
-    if num_labels > L.nbg_group_cols_max_labels(_COLS_FUNCS[name]):
+    if num_labels > L.nbg_group_cols_max_labels(_lib.GROUP_FUNC_IDS[name]):
         return None
     outer = math.prod(v.shape[:k0])
     m = math.prod(v.shape[k0 : axes[-1] + 1])
@@ -182,7 +182,7 @@ def _group_columns(name, v, lab, moved_axes, num_labels, ddof):
     out = torch.empty(tuple(v.shape[:k0]) + tuple(v.shape[axes[-1] + 1 :]) + (num_labels,), dtype=v.dtype,
                       device=v.device)
     if out.numel():
-        fn = getattr(L, f"nbg_group_{name}_cols_f64_{'i64' if lab_dt == torch.int64 else 'i32'}")
+        fn = getattr(L, f"nbg_group_{name}_cols_{_COLS_DTYPES[v.dtype]}_{'i64' if lab_dt == torch.int64 else 'i32'}")
         _lib.check(fn(v.data_ptr() if m else None, flat_lab.data_ptr() if m else None, out.data_ptr(), outer, m, inner,
                       num_labels, int(ddof), _host.stream(v.device)), f"group_{name}")
     return out

@@ -91,6 +91,28 @@ def test_group_partial_row_block(fname):
     _check_group(fname, values, labels, 4096, f"{fname} 17 rows")
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64])
+@pytest.mark.parametrize("fname", ["group_nanargmax", "group_nanargmin", "group_nanmax", "group_nanmin"])
+def test_group_large_k_selection_ties(fname, dtype):
+    # K = 200,000 takes the one-pass (key, column) pair updates in L2.  Values from seven
+    # levels make nearly every bin a tie that the smallest column must win (signed zeros
+    # included, which compare equal), and one label holding a tenth of the columns makes
+    # its bins contended, so swaps race and retry.
+    rng = np.random.default_rng(45)
+    rows, m, K = 8, 400_000, 200_000
+    x = rng.integers(-3, 4, size=(rows, m)).astype(dtype)
+    if np.issubdtype(dtype, np.floating):
+        x[(x == 0) & (rng.random(x.shape) < 0.5)] = -0.0
+        x[rng.random(x.shape) < 0.05] = np.nan
+    labels = rng.integers(0, K, size=m).astype(np.int32)
+    labels[rng.random(m) < 0.1] = 7
+    labels[rng.random(m) < 0.01] = -1
+    got = getattr(nb, fname)(torch.from_numpy(x).cuda(), torch.from_numpy(labels).cuda(), num_labels=K,
+                             axis=-1).cpu().numpy()
+    want = oracle.group(fname, x, labels, num_labels=K, axis=-1)
+    assert_bit_equal(got, want, f"{fname} {np.dtype(dtype)} K={K}")
+
+
 @pytest.mark.parametrize("fname", ["group_nanvar", "group_nansum", "group_nanargmax"])
 def test_group_eight_rows_per_block(fname):
     # K = 300,000: a variance's 20 bytes per (row, label) fit eight rows in a block

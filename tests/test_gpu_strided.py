@@ -162,15 +162,30 @@ def test_flox_style_grouped_calls():
             np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12, err_msg=f)
 
 
-@pytest.mark.parametrize("fname", ["group_nansum", "group_nanmean", "group_nancount", "group_nanvar", "group_nanstd"])
-def test_group_non_last_axes_bit_exact(fname):
-    # float64 values grouped over consecutive leading / middle axes: one thread per column
-    # runs numbagg's loop in place, so the sums are the reference's bit for bit
+_GROUP_FUNCS = [
+    "group_nansum", "group_nanmean", "group_nancount", "group_nanvar", "group_nanstd", "group_nansum_of_squares",
+    "group_nanprod", "group_nanargmax", "group_nanargmin", "group_nanmax", "group_nanmin", "group_nanfirst",
+    "group_nanlast", "group_nanany", "group_nanall",
+]
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64])
+@pytest.mark.parametrize("fname", _GROUP_FUNCS)
+def test_group_non_last_axes_bit_exact(fname, dtype):
+    # values grouped over consecutive leading / middle axes: one thread per column runs
+    # numbagg's loop in place, so every function's results are the reference's bit for
+    # bit (float sums rounded per addition, integer sums and products wrapping)
     rng = np.random.default_rng(44)
     cases = [((700, 4096), 0, 12), ((3, 40, 50, 2100), (1, 2), 7), ((5, 300, 2048), 1, 30)]
     for shape, axis, K in cases:
-        x = rng.standard_normal(shape) * 3 + 1
-        x[rng.random(shape) < 0.1] = np.nan
+        if np.issubdtype(dtype, np.floating):
+            x = (rng.standard_normal(shape) * 3 + 1).astype(dtype)
+            if fname == "group_nanprod":
+                x = (1 + 0.01 * rng.standard_normal(shape)).astype(dtype)
+            x[rng.random(shape) < 0.1] = np.nan
+            x[rng.random(shape) < 0.05] = 0
+        else:
+            x = rng.integers(-40, 40, size=shape).astype(dtype)
         ax = (axis,) if isinstance(axis, int) else axis
         lshape = tuple(shape[a] for a in ax)
         labels = rng.integers(-1, K + 2, size=lshape)  # negative and >= num_labels skipped
@@ -179,8 +194,10 @@ def test_group_non_last_axes_bit_exact(fname):
         kw = {"ddof": 0} if fname in ("group_nanvar", "group_nanstd") else {}
         got = getattr(nb, fname)(xt, lt, axis=axis, num_labels=K, **kw).cpu().numpy()
         want = oracle.group(fname, x, labels, axis=axis, num_labels=K, **kw)
-        assert got.shape == want.shape, (shape, axis)
-        assert_bit_equal(got, want, f"{fname} {shape} axis={axis}")
+        assert got.shape == want.shape and got.dtype == want.dtype, (shape, axis, got.dtype, want.dtype)
+        assert_bit_equal(got, want, f"{fname} {np.dtype(dtype)} {shape} axis={axis}")
+    if dtype is not np.float64:
+        return
     # more labels than the shared-memory bins hold: the moved-axis path, same values
     x = rng.standard_normal((200, 2048))
     labels = rng.integers(0, 3000, size=200)
