@@ -328,8 +328,7 @@ NBG_DECL_GROUP_ALL(nanall)            /* numbagg/grouped.py:260-270 */
  * numbagg's np.ndindex order); out[(o * inner + i) * K + k], in the values dtype like the
  * row entry points above.  One thread per column runs numbagg's loop, so the results are
  * the reference's bit for bit.  No workspace; K at most nbg_group_cols_max_labels(func)
- * (func: 0 sum, 1 mean, 2 count, 3 var, 4 std, 5 sum_of_squares, 6 prod, 7 argmax,
- * 8 argmin, 9 max, 10 min, 11 first, 12 last, 13 any, 14 all), else NBG_UNSUPPORTED.
+ * (func numbered as for nbg_group_workspace_bytes), else NBG_UNSUPPORTED.
  * nanmean/nanvar/nanstd take float values only (numbagg computes integers in float64). */
 NBG_API size_t nbg_group_cols_max_labels(int func);
 #define NBG_DECL_GROUP_COLS1(NAME, V, VS, L, LS)                                                 \

@@ -64,6 +64,9 @@ def test_invalid_arguments_are_rejected_before_launch(lib):
     assert lib.nbg_move_std_cols_f64(null, null, 1, 10, 4, 0, 3, null) == 1
     assert lib.nbg_move_corr_cols_f32(null, null, null, 1, 10, 4, 3, -1, null) == 1
     assert lib.nbg_move_mean_cols_f64(null, null, 0, 10, 4, 3, 3, null) == 0
+    assert lib.nbg_group_nanargmax_cols_i32_i64(null, null, null, 1, -1, 4, 3, 1, null) == 1
+    assert lib.nbg_group_nanvar_cols_f32_i32(null, null, null, 0, 10, 4, 3, 1, null) == 0
+    assert lib.nbg_group_nansum_cols_f64_i32(null, null, null, 2, 10, 4, 97, 1, null) == 1  # no output
     # empty problems succeed without work
     assert lib.nbg_move_mean_f64(null, null, 0, 10, 3, 3, null, 0, null) == 0
     assert lib.nbg_ffill_f32(null, null, 3, 0, 2, null, 0, null) == 0
@@ -79,6 +82,15 @@ def test_workspace_queries(lib):
     assert lib.nbg_fill_workspace_bytes(64, 1 << 24) > lib.nbg_fill_workspace_bytes(64, 1 << 10)
     assert lib.nbg_group_workspace_bytes(0, 4, 1000, 16) >= 4 * 16 * 24
     assert lib.nbg_group_workspace_bytes(99, 4, 1000, 16) == 0
+    # in-place grouped column kernels: shared-memory bins of 8, 16 or 24 bytes per
+    # (label, column) for 128 columns within 96 KB (numbering of nbg_group_workspace_bytes)
+    ids = {"nansum": 0, "nancount": 1, "nanmean": 2, "nanvar": 3, "nanstd": 4, "nanargmax": 6, "nanmax": 8,
+           "nanfirst": 10, "nanlast": 11, "nanprod": 12, "nanall": 14}
+    want = {"nansum": 96, "nancount": 96, "nanmean": 48, "nanvar": 32, "nanstd": 32, "nanargmax": 48, "nanmax": 48,
+            "nanfirst": 48, "nanlast": 96, "nanprod": 96, "nanall": 96}
+    for name, fid in ids.items():
+        assert lib.nbg_group_cols_max_labels(fid) == want[name], name
+    assert lib.nbg_group_cols_max_labels(15) == 0 and lib.nbg_group_cols_max_labels(-1) == 0
 
 
 @pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])

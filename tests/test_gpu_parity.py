@@ -225,12 +225,15 @@ def test_move_exp_min_weight(fname):
         assert np.sum(~np.isnan(func(array, min_weight=mw, alpha=alpha))[6:]) == expected, (mw, alpha)
 
 
+# n = 100,003: odd rows, so every other row starts off a 16-byte boundary; n = 100,000:
+# aligned rows with a partial last tile; n = 57,344: whole 4,096-position tiles only
+@pytest.mark.parametrize("n", [100_003, 100_000, 57_344])
 @pytest.mark.parametrize("fname", ["ffill", "bfill"])
 @pytest.mark.parametrize("limit", [None, 0, 1, 5, 10_000])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_fill_vs_oracle(fname, limit, dtype):
+def test_fill_vs_oracle(fname, limit, dtype, n):
     rng = np.random.default_rng(10)
-    x = rng.standard_normal((5, 100_003)).astype(dtype)
+    x = rng.standard_normal((5, n)).astype(dtype)
     x[rng.random(x.shape) < 0.3] = np.nan
     x[2, 1000:60_000] = np.nan  # runs across many tiles
     x[3] = np.nan
