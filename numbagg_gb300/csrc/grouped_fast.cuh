@@ -174,6 +174,16 @@ NBG_DEVICE Dec decomp(long long x) {
   return decomp(static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
 }
 
+// infinity and sign tests on the bits (integers: never infinite)
+NBG_DEVICE bool inf_bits(unsigned long long b) { return (b << 1) == 0xffe0000000000000ull; }
+NBG_DEVICE bool inf_bits(unsigned b) { return (b << 1) == 0xff000000u; }
+NBG_DEVICE bool inf_bits(int) { return false; }
+NBG_DEVICE bool inf_bits(long long) { return false; }
+NBG_DEVICE bool sign_bit(unsigned long long b) { return (b >> 63) != 0; }
+NBG_DEVICE bool sign_bit(unsigned b) { return (b >> 31) != 0; }
+NBG_DEVICE bool sign_bit(int v) { return v < 0; }
+NBG_DEVICE bool sign_bit(long long v) { return v < 0; }
+
 // the value of a bit pattern as float64
 NBG_DEVICE double bits_to_f64(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
 NBG_DEVICE double bits_to_f64(unsigned b) { return static_cast<double>(__int_as_float(static_cast<int>(b))); }
@@ -207,13 +217,16 @@ NBG_DEVICE unsigned long long sel_key_of(V v) {
 // A warp keeps a scale exponent E, the largest biased exponent among the finite values
 // it has met (it only grows), and every lane keeps its own K bins in shared memory:
 //   value  x   -> +-(m >> (E - e + d1))          LSB 2^(E + d1 - 1075)
-//   square x^2 -> (m*m) >> (2(E - e) + d2)        LSB 2^(2E + d2 - 2150)
-// d1, d2 come from the host: with n the number of elements one lane can meet in its
-// chunk (< 2^lg), d1 = max(0, lg - 10) and d2 = 43 + lg, so a lane's sums stay below
-// 2^63.  When E grows, each lane shifts its own bins down.  Bits below the LSB are
-// truncated: at most 2^-(52 - d1) of the largest value the warp met, per term.
-// At the end of the chunk the lanes' bins are summed exactly (128-bit) per warp and
-// rounded once to float64.
+// d1 comes from the host: with n the number of elements one lane can meet in its chunk
+// (< 2^lg), d1 = max(0, lg - 10), so a lane's sums stay below 2^63.  When E grows, each
+// lane shifts its own bins down.  Bits below the LSB are truncated: at most
+// 2^-(52 - d1) of the largest value the warp met, per term.  At the end of the chunk the
+// lanes' bins are summed exactly (128-bit) per warp and rounded once to float64.
+// Squares go to float64 lane bins (one fused multiply-add each on the FP64 pipe, which
+// the integer work leaves idle; a 64 x 64-bit product and a 128-bit shift per element
+// made the variance the slowest of these kernels), reduced in a fixed order per warp:
+// each rounding chain is one lane's elements of one chunk, far shorter than the
+// reference's sequential sum over the row.
 // CTAs per SM the tiny moment kernels are compiled for: sums and means are bound by
 // integer issue and gain from a third CTA; the others measured faster with two
 template <int F>
@@ -221,18 +234,39 @@ struct TinyOcc {
   static constexpr int value = (F == kSum || F == kMean) ? 3 : 2;
 };
 
-template <int F, typename V, typename L>
+// SPLIT (sums and means): three of every four elements of a lane's tile go to float64
+// lane bins instead of the fixed-point ones (one float64 add on the FP64 pipe, no
+// decomposition or shift); the counts of a split mean are 16-bit (the host keeps a
+// lane's elements per chunk below 2^16).  The variances do not split: their squares
+// already keep the FP64 pipe busy (measured 3.72 ms unsplit, 3.88 ms split at K = 16).
+// The float64 bins add in a fixed order per lane and are reduced in a fixed order, so
+// results stay reproducible, within about 2^-53 times a lane's element count of the
+// sum of magnitudes.
+template <int F, bool SPLIT>
+struct TinyCount {
+  typedef int type;
+};
+template <int F>
+struct TinyCount<F, true> {
+  typedef unsigned short type;
+};
+
+template <int F, typename V, typename L, bool SPLIT>
 __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                          long long rows, long long m, int K, long long chunk_len,
-                                                         long long chunks, int d1, int d2,
+                                                         long long chunks, int d1,
                                                          MomPart* __restrict__ parts) {
   typedef typename BitsOf<V>::type B;
+  typedef typename TinyCount<F, SPLIT>::type C;
   constexpr bool S1 = Need<F>::s1, S2 = Need<F>::s2, CNT = Need<F>::cnt, VL = Need<F>::varlike;
   constexpr bool MOM = S1 || S2;
+  static_assert(!SPLIT || (S1 && !S2), "the split is for sums and means");
+  constexpr int FMASK = 3;  // elements j of a lane's tile with (j & FMASK) != 0 take the float64 bins
   extern __shared__ __align__(16) unsigned char smem_raw[];
   long long* b1 = reinterpret_cast<long long*>(smem_raw);  // [K][FT]
-  unsigned long long* b2 = reinterpret_cast<unsigned long long*>(smem_raw + (S1 ? K * FT * 8 : 0));
-  int* bc = reinterpret_cast<int*>(smem_raw + (S1 ? K * FT * 8 : 0) + (S2 ? K * FT * 8 : 0));
+  double* f2 = reinterpret_cast<double*>(smem_raw + (S1 ? K * FT * 8 : 0));  // squares, float64
+  double* f1 = reinterpret_cast<double*>(smem_raw + (S1 ? K * FT * 8 : 0) + (S2 ? K * FT * 8 : 0));
+  C* bc = reinterpret_cast<C*>(smem_raw + (S1 ? K * FT * 8 : 0) + (S2 ? K * FT * 8 : 0) + (SPLIT ? K * FT * 8 : 0));
   __shared__ double wsum1[FT / 32][kTinyK], wsum2[FT / 32][kTinyK];
   __shared__ int wcnt[FT / 32][kTinyK];
   __shared__ int infs[2][kTinyK];
@@ -243,7 +277,8 @@ __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V
   const long long c1 = min(m, c0 + chunk_len);
   for (int k = 0; k < K; ++k) {
     if (S1) b1[k * FT + tid] = 0;
-    if (S2) b2[k * FT + tid] = 0;
+    if (S2) f2[k * FT + tid] = 0.0;
+    if (SPLIT) f1[k * FT + tid] = 0.0;
     if (CNT) bc[k * FT + tid] = 0;
   }
   if (tid < 2 * kTinyK) infs[tid / kTinyK][tid % kTinyK] = 0;
@@ -275,20 +310,19 @@ __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V
 #pragma unroll
     for (int j = 0; j < J; ++j) {
       if (nan_bits(v[j])) lab[j] = -1;
-      if (MOM) {
+      if (S1 && !(SPLIT && (j & FMASK) != 0)) {
         const Dec d = decomp(v[j]);
         if (lab[j] >= 0 && !d.special && !(VL && d.e >= 1023 + 512)) emax = max(emax, d.e);
       }
     }
-    if (MOM) {
+    if (S1) {
       const int Et = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(emax)));
       if (Et > E) {  // uniform: the warp's scale grows
         if (E > 0) {
           const int dd = Et - E;
           for (int k = 0; k < K; ++k) {
             const int slot = k * FT + tid;
-            if (S1) b1[slot] = dd >= 63 ? (b1[slot] < 0 ? -1ll : 0ll) : (b1[slot] >> dd);
-            if (S2) b2[slot] = 2 * dd >= 64 ? 0ull : (b2[slot] >> (2 * dd));
+            b1[slot] = dd >= 63 ? (b1[slot] < 0 ? -1ll : 0ll) : (b1[slot] >> dd);
           }
         }
         E = Et;
@@ -300,6 +334,14 @@ __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V
       const int slot = lab[j] * FT + tid;
       if (CNT) bc[slot] += 1;
       if (!MOM) continue;
+      if (SPLIT && (j & FMASK) != 0) {
+        if (inf_bits(v[j])) {
+          atomicAdd(&infs[sign_bit(v[j]) ? 1 : 0][lab[j]], 1);
+          continue;
+        }
+        f1[slot] += bits_to_f64(v[j]);
+        continue;
+      }
       const Dec d = decomp(v[j]);
       if (d.special || (VL && d.e >= 1023 + 512)) {  // infinity, or a square that overflows
         atomicAdd(&infs[d.neg ? 1 : 0][lab[j]], 1);
@@ -311,13 +353,8 @@ __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V
         b1[slot] += d.neg ? -static_cast<long long>(a) : static_cast<long long>(a);
       }
       if (S2) {
-        const int sh = 2 * (E - d.e) + d2;  // >= d2 >= 43
-        unsigned long long q = 0ull;
-        if (sh < 106) {
-          const unsigned long long lo = d.m * d.m, hi = __umul64hi(d.m, d.m);
-          q = sh >= 64 ? (hi >> (sh - 64)) : ((hi << (64 - sh)) | (lo >> sh));
-        }
-        b2[slot] += q;
+        const double x = bits_to_f64(v[j]);
+        f2[slot] = fma(x, x, f2[slot]);
       }
     }
 #pragma unroll
@@ -341,21 +378,20 @@ __global__ void __launch_bounds__(FT, TinyOcc<F>::value) tiny_mom_kernel(const V
         hi = hi + ohi + (nlo < lo ? 1 : 0);
         lo = nlo;
       }
-      if (lane == 0)
-        wsum1[warp][k] = fx::to_double((static_cast<fx::i128>(hi) << 64) + static_cast<fx::i128>(lo), E + d1 - 1075);
-    }
-    if (S2) {
-      unsigned long long lo = b2[slot], hi = 0ull;
+      double fs = 0.0;
+      if (SPLIT) {
+        fs = f1[slot];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, o);
-        const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, hi, o);
-        const unsigned long long nlo = lo + olo;
-        hi = hi + ohi + (nlo < lo ? 1ull : 0ull);
-        lo = nlo;
+        for (int o = 16; o > 0; o >>= 1) fs += __shfl_xor_sync(0xffffffffu, fs, o);
       }
       if (lane == 0)
-        wsum2[warp][k] = fx::to_double(static_cast<fx::i128>((static_cast<fx::u128>(hi) << 64) | lo), 2 * E + d2 - 2150);
+        wsum1[warp][k] = fx::to_double((static_cast<fx::i128>(hi) << 64) + static_cast<fx::i128>(lo), E + d1 - 1075) + fs;
+    }
+    if (S2) {
+      double q = f2[slot];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+      if (lane == 0) wsum2[warp][k] = q;
     }
     if (CNT) {
       const int c = static_cast<int>(__reduce_add_sync(0xffffffffu, static_cast<unsigned>(bc[slot])));
@@ -1404,16 +1440,20 @@ int launch_fast(const V* values, const L* labels, O* out, long long rows, long l
   if (is_moments(F)) {
     if (p.strategy == 0) {
       MomPart* parts = carve<MomPart>(cur, rows * p.chunks * K);
-      const size_t smem = static_cast<size_t>(K) * FT * ((Need<F>::s1 ? 8 : 0) + (Need<F>::s2 ? 8 : 0) + (Need<F>::cnt ? 4 : 0));
       // headroom of the lanes' fixed-point sums (see tiny_mom_kernel)
       const long long per_lane = ((p.chunk_len + kTileCols * (FT / 32) - 1) / (kTileCols * (FT / 32))) * 16;
       int lg = 0;
       while ((1ll << lg) < per_lane) ++lg;
-      const int d1 = lg > 10 ? lg - 10 : 0, d2 = 43 + lg;
-      auto kern = tiny_mom_kernel<F, V, L>;
+      const int d1 = lg > 10 ? lg - 10 : 0;
+      constexpr bool can_split = F == kSum || F == kMean;
+      const bool split = can_split && per_lane < 65536;
+      const size_t smem = static_cast<size_t>(K) * FT *
+                          ((Need<F>::s1 ? 8 : 0) + (Need<F>::s2 ? 8 : 0) + (split ? 8 : 0) +
+                           (Need<F>::cnt ? (split ? 2 : 4) : 0));
+      auto kern = split ? tiny_mom_kernel<F, V, L, can_split> : tiny_mom_kernel<F, V, L, false>;
       set_smem(kern, smem);
       kern<<<static_cast<int>(nctas), FT, smem, s>>>(values, labels, rows, m, static_cast<int>(K), p.chunk_len, p.chunks,
-                                                     d1, d2, parts);
+                                                     d1, parts);
       fold_mom_kernel<F, O><<<fin_grid(rows * K), 256, 0, s>>>(parts, out, rows, K, p.chunks, ddof);
       launches += 2;
     } else if (p.strategy == 1) {

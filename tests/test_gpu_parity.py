@@ -286,6 +286,40 @@ def test_group_vs_oracle(fname, K):
         assert_scaled_close(got, want, scale, F64_TOL, None, fname)
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("fname", ["group_nansum", "group_nanmean", "group_nanvar", "group_nansum_of_squares"])
+def test_group_few_labels_infinities(fname, dtype):
+    # K <= 16 (lane-private bins): a lane's elements alternate between its fixed-point
+    # and (for sums and means) float64 bins, so infinities land at every position of a
+    # tile; label 0 holds +inf, label 1 -inf, label 2 both (NaN), the rest finite
+    rng = np.random.default_rng(16)
+    m, K = 300_000, 8
+    values = rng.standard_normal((4, m)).astype(dtype)
+    values[rng.random(values.shape) < 0.05] = np.nan
+    labels = rng.integers(0, K, size=m).astype(np.int32)
+    cols0 = np.flatnonzero(labels == 0)[:40]
+    cols1 = np.flatnonzero(labels == 1)[:40]
+    cols2 = np.flatnonzero(labels == 2)[:40]
+    values[:, cols0[::3]] = np.inf
+    values[:, cols1[1::3]] = -np.inf
+    values[:, cols2[::5]] = np.inf
+    values[:, cols2[2::5]] = -np.inf
+    got = getattr(nb, fname)(values, labels, num_labels=K, axis=-1)
+    want = oracle.group(fname, values, labels, num_labels=K, axis=-1)
+    assert np.array_equal(np.isnan(got), np.isnan(want)), fname
+    assert np.array_equal(np.isposinf(got), np.isposinf(want)) and np.array_equal(np.isneginf(got), np.isneginf(want))
+    fin = np.isfinite(want)
+    v64 = np.where(np.isfinite(values), values, 0.0).astype(np.float64)
+    s1 = np.stack([np.bincount(labels, weights=np.abs(v64[r]), minlength=K) for r in range(4)])
+    s2 = np.stack([np.bincount(labels, weights=v64[r] ** 2, minlength=K) for r in range(4)])
+    cnt = np.stack([np.bincount(labels, weights=(~np.isnan(values[r])).astype(float), minlength=K) for r in range(4)])
+    scale = {"group_nansum": s1, "group_nanmean": s1 / np.maximum(cnt, 1), "group_nanvar": s2 / np.maximum(cnt, 1),
+             "group_nansum_of_squares": s2}[fname]
+    # float32: the reference accumulates in float32 over ~37,000 terms per group
+    tol = 1e-4 if dtype == np.float32 else F64_TOL
+    assert_scaled_close(got[fin], want[fin], scale[fin], tol, None, f"{fname} {np.dtype(dtype)}")
+
+
 @pytest.mark.parametrize("dtype", [np.int32, np.int64, np.float32, np.bool_])
 @pytest.mark.parametrize("fname", [f.__name__ for f in nb.GROUPED_FUNCS])
 def test_group_dtypes(fname, dtype):
