@@ -159,28 +159,41 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
 _COLS_DTYPES = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
 
 
+def group_columns_layout(shape, moved_axes):
+    """(outer, m, inner) when the reduced axes are consecutive, increasing and not last
+    (a C-contiguous array is then `outer` blocks of m x `inner` values, the labels
+    running over m) and there are enough columns for the column kernel; else None."""
+    if not moved_axes:
+        return None
+    axes = tuple(moved_axes)
+    k0 = axes[0]
+    if axes != tuple(range(k0, k0 + len(axes))) or axes[-1] >= len(shape) - 1:
+        return None
+    outer = math.prod(shape[:k0])
+    m = math.prod(shape[k0 : axes[-1] + 1])
+    inner = math.prod(shape[axes[-1] + 1 :])
+    if outer * inner < _host.MIN_COLUMNS:
+        return None
+    return outer, m, inner
+
+
 def _group_columns(name, v, lab, moved_axes, num_labels, ddof):
     """Values reduced over consecutive, increasing, non-last axes of a C-contiguous
     array: one thread per column runs numbagg's loop in place (no copy, the reference's
     results bit for bit).  None when that does not apply."""
-    if v.dtype not in _COLS_DTYPES or not moved_axes or not v.is_contiguous():
+    if v.dtype not in _COLS_DTYPES or not v.is_contiguous():
         return None
-    axes = tuple(moved_axes)
-    k0 = axes[0]
-    if axes != tuple(range(k0, k0 + len(axes))) or axes[-1] >= v.ndim - 1:
+    layout = group_columns_layout(tuple(v.shape), moved_axes)
+    if layout is None:
         return None
     L = _lib.lib()
     if num_labels > L.nbg_group_cols_max_labels(_lib.GROUP_FUNC_IDS[name]):
         return None
-    outer = math.prod(v.shape[:k0])
-    m = math.prod(v.shape[k0 : axes[-1] + 1])
-    inner = math.prod(v.shape[axes[-1] + 1 :])
-    if outer * inner < _host.MIN_COLUMNS:
-        return None
+    outer, m, inner = layout
+    k0, k1 = moved_axes[0], moved_axes[-1]
     lab_dt = torch.int64 if lab.dtype == torch.int64 else torch.int32
     flat_lab = lab.to(lab_dt).contiguous().reshape(m)
-    out = torch.empty(tuple(v.shape[:k0]) + tuple(v.shape[axes[-1] + 1 :]) + (num_labels,), dtype=v.dtype,
-                      device=v.device)
+    out = torch.empty(tuple(v.shape[:k0]) + tuple(v.shape[k1 + 1 :]) + (num_labels,), dtype=v.dtype, device=v.device)
     if out.numel():
         fn = getattr(L, f"nbg_group_{name}_cols_{_COLS_DTYPES[v.dtype]}_{'i64' if lab_dt == torch.int64 else 'i32'}")
         _lib.check(fn(v.data_ptr() if m else None, flat_lab.data_ptr() if m else None, out.data_ptr(), outer, m, inner,

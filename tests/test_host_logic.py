@@ -150,3 +150,13 @@ def test_in_place_layouts():
     assert middle_inner((4, 40, 50, 64), (2, 3)) is None  # includes the last axis
     assert middle_inner((400, 8), (0,)) is None  # fewer outputs than a warp
     assert middle_inner((5,), ()) is None
+    # grouped reductions: consecutive increasing reduced axes, not the last one
+    from numbagg_gb300.grouped import group_columns_layout
+
+    assert group_columns_layout((700, 4096), (0,)) == (1, 700, 4096)
+    assert group_columns_layout((3, 40, 50, 2100), (1, 2)) == (3, 2000, 2100)
+    assert group_columns_layout((3, 40, 50, 2100), (2, 1)) is None  # the labels' order would change
+    assert group_columns_layout((3, 40, 50, 2100), (2, 3)) is None  # includes the last axis
+    assert group_columns_layout((3, 40, 50, 2100), (0, 2)) is None  # not consecutive
+    assert group_columns_layout((700, 8), (0,)) is None  # too few columns
+    assert group_columns_layout((700, 4096), None) is None  # labels over every axis
