@@ -83,12 +83,24 @@ def rows_last(t: torch.Tensor, axis: int) -> tuple[torch.Tensor, tuple[int, ...]
     return flat, shape
 
 
-# fewest columns for the one-thread-per-column kernels: below this a non-last axis is
-# moved last and copied instead (too few threads would keep the GPU idle)
+# The one-thread-per-column kernels walk each column serially (0.2 us a position for a
+# fill, about 0.5 for a grouped reduction, 0.8-1.1 for a moving window or an EWM, which
+# run numbagg's float64 loop), so they need many columns to beat moving the axis last
+# with a copy and running the row kernels.  Measured on a GB300, float64 along axis 0:
+# 16,384 x 8,192 took 1.06 / 3.36 / 4.46 / 1.28 ms (fill / move_mean / EWM mean / grouped
+# sum) through the copy against 3.2 / 13.0 / 17.6 / 7.3 ms in place; 2,048 x 65,536 took
+# 1.26 / 3.57 / 4.47 / 4.26 ms through the copy against 0.54 / 3.11 / 4.38 / 0.93 ms in
+# place.  The crossover is near 256 KB of columns per position.
 MIN_COLUMNS = 2048
+COLUMN_MIN_ROW_BYTES = 256 * 1024
 
 
-def column_layout(t: torch.Tensor, axis: int) -> tuple[int, int, int] | None:
+def column_min(itemsize: int) -> int:
+    """Fewest columns for the in-place column kernels at this element size."""
+    return max(MIN_COLUMNS, COLUMN_MIN_ROW_BYTES // max(int(itemsize), 1))
+
+
+def column_layout(t: torch.Tensor, axis: int, min_columns: int | None = None) -> tuple[int, int, int] | None:
     """(outer, n, inner) when `t` is C-contiguous and `axis` is not its last axis: the
     array is then `outer` blocks of n x `inner` values, and a kernel with one thread per
     column scans it along `axis` in place, with no copy (numbagg's gufuncs take such
@@ -102,7 +114,7 @@ def column_layout(t: torch.Tensor, axis: int) -> tuple[int, int, int] | None:
     inner = 1
     for d in t.shape[axis + 1 :]:
         inner *= int(d)
-    if outer * inner < MIN_COLUMNS:
+    if outer * inner < (column_min(t.element_size()) if min_columns is None else min_columns):
         return None
     return outer, int(t.shape[axis]), inner
 

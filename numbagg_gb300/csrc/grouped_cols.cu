@@ -132,40 +132,63 @@ __global__ void __launch_bounds__(NT) group_cols_kernel(const V* __restrict__ va
   if (col >= outer * inner) return;
   const long long o = col / inner, i = col - o * inner;
   const V* vc = values + o * m * inner + i;
-  for (long long r = 0; r < m; ++r) {
-    const long long lab = static_cast<long long>(__ldg(labels + r));
-    if (lab < 0 || lab >= K) continue;
-    const V x = __ldg(vc + r * inner);
-    if (A::isnan_(x)) continue;
-    const int slot = static_cast<int>(lab) * NT + tid;
-    V& a = sa[slot * SA];
-    if (F == kSum) a = A::add(a, x);
-    if (F == kSumSq) a = A::add(a, A::mul(x, x));
-    if (F == kProd) a = A::mul(a, x);
-    if (F == kCount) a = A::add(a, V(1));
-    if (F == kMean || F == kVar || F == kStd) {
-      a = A::add(a, x);
-      sc[slot] += 1;
-      if (F != kMean) {  // var's sum of squares in V, kept in the float64 word
-        V* q = reinterpret_cast<V*>(sb + slot);
-        *q = A::add(*q, A::mul(x, x));
+  // a ring of the next D positions' values and labels, so D loads are in flight while
+  // one position is reduced (a thread's walk is serial: the ring is its parallelism)
+  constexpr int D = 8;
+  V ring[D];
+  int lring[D];  // the label, or -1 where it is skipped
+  auto label_at = [&](long long r) {
+    const long long l = static_cast<long long>(__ldg(labels + r));
+    return (l < 0 || l >= K) ? -1 : static_cast<int>(l);
+  };
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    ring[d] = d < m ? __ldg(vc + d * inner) : V(0);
+    lring[d] = d < m ? label_at(d) : -1;
+  }
+  for (long long r0 = 0; r0 < m; r0 += D) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const long long r = r0 + d;
+      if (r >= m) break;
+      const V x = ring[d];
+      const int lab = lring[d];
+      if (r + D < m) {
+        ring[d] = __ldg(vc + (r + D) * inner);
+        lring[d] = label_at(r + D);
       }
-    }
-    if (EXT) {  // numbagg/grouped.py:54-92, :211-244: float64 comparison, first index on ties
-      const double xd = static_cast<double>(x);
-      const double e = sb[slot];
-      if (is_nan(e) || (MAXI ? xd > e : xd < e)) {
-        sb[slot] = xd;
-        if (F == kArgMax || F == kArgMin) a = static_cast<V>(r);
+      if (lab < 0) continue;
+      if (A::isnan_(x)) continue;
+      const int slot = lab * NT + tid;
+      V& a = sa[slot * SA];
+      if (F == kSum) a = A::add(a, x);
+      if (F == kSumSq) a = A::add(a, A::mul(x, x));
+      if (F == kProd) a = A::mul(a, x);
+      if (F == kCount) a = A::add(a, V(1));
+      if (F == kMean || F == kVar || F == kStd) {
+        a = A::add(a, x);
+        sc[slot] += 1;
+        if (F != kMean) {  // var's sum of squares in V, kept in the float64 word
+          V* q = reinterpret_cast<V*>(sb + slot);
+          *q = A::add(*q, A::mul(x, x));
+        }
       }
+      if (EXT) {  // numbagg/grouped.py:54-92, :211-244: float64 comparison, first index on ties
+        const double xd = static_cast<double>(x);
+        const double e = sb[slot];
+        if (is_nan(e) || (MAXI ? xd > e : xd < e)) {
+          sb[slot] = xd;
+          if (F == kArgMax || F == kArgMin) a = static_cast<V>(r);
+        }
+      }
+      if (F == kFirst && sc[slot] == 0) {
+        sc[slot] = 1;
+        a = x;
+      }
+      if (F == kLast) a = x;
+      if (F == kAny && x != V(0)) a = V(1);
+      if (F == kAll && x == V(0)) a = V(0);
     }
-    if (F == kFirst && sc[slot] == 0) {
-      sc[slot] = 1;
-      a = x;
-    }
-    if (F == kLast) a = x;
-    if (F == kAny && x != V(0)) a = V(1);
-    if (F == kAll && x == V(0)) a = V(0);
   }
   V* oc = out + col * K;
   for (int k = 0; k < K; ++k) {

@@ -1099,6 +1099,7 @@ __global__ void __launch_bounds__(256) move_cols_kernel(const T* __restrict__ a,
     long long count = 0;
     const long long w0 = window < n ? window : n;
     for (long long p = 0; p < w0; ++p) {
+      if (p + kColPrefetch < n) prefetch_l2(ac + (p + kColPrefetch) * inner);
       const double ai = ld_col(ac + p * inner);
       if (!isnan_d(ai)) {
         asum = __dadd_rn(asum, ai);
@@ -1107,6 +1108,7 @@ __global__ void __launch_bounds__(256) move_cols_kernel(const T* __restrict__ a,
       oc[p * inner] = static_cast<T>(count >= mc ? (OP == kMean ? __ddiv_rn(asum, static_cast<double>(count)) : asum) : nan);
     }
     for (long long p = window; p < n; ++p) {
+      if (p + kColPrefetch < n) prefetch_l2(ac + (p + kColPrefetch) * inner);
       const double ai = ld_col(ac + p * inner);
       const double aold = ld_col(ac + (p - window) * inner);
       if (OP == kMean) {  // removes the old value first
@@ -1137,6 +1139,7 @@ __global__ void __launch_bounds__(256) move_cols_kernel(const T* __restrict__ a,
     double asum = 0.0, asum_sq = 0.0;
     long long count = 0;
     for (long long p = 0; p < n; ++p) {
+      if (p + kColPrefetch < n) prefetch_l2(ac + (p + kColPrefetch) * inner);
       const double ai = ld_col(ac + p * inner);
       if (p >= window) {
         const double aold = ld_col(ac + (p - window) * inner);
@@ -1166,6 +1169,10 @@ __global__ void __launch_bounds__(256) move_cols_kernel(const T* __restrict__ a,
   double asum = 0.0, bsum = 0.0, prodsum = 0.0, asum_sq = 0.0, bsum_sq = 0.0;
   long long count = 0;
   for (long long p = 0; p < n; ++p) {
+    if (p + kColPrefetch < n) {
+      prefetch_l2(ac + (p + kColPrefetch) * inner);
+      prefetch_l2(bc + (p + kColPrefetch) * inner);
+    }
     const double ai = ld_col(ac + p * inner), bi = ld_col(bc + p * inner);
     if (p >= window) {
       const double aold = ld_col(ac + (p - window) * inner), bold = ld_col(bc + (p - window) * inner);

@@ -103,6 +103,11 @@ NBG_DEVICE void red_add_hint(unsigned* a, unsigned v, unsigned long long pol) {
   asm volatile("red.global.add.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
 }
 
+// Ask L2 for a line ahead of its use (no register, no fault on a valid address); the
+// column kernels walk a column serially, so this is their memory-level parallelism.
+NBG_DEVICE void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+constexpr long long kColPrefetch = 16;  // positions ahead
+
 // Values handled as raw bits.  Loading a float array through its integer twin keeps
 // every test on the integer pipes: a NaN test on a float64 register can be compiled
 // to a float64 compare, and this GPU's FP64 pipe takes 16 cycles per warp instruction.

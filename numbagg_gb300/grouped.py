@@ -159,10 +159,11 @@ def _group(name, values, labels, *, ddof=1, num_labels=None, axis=None):
 _COLS_DTYPES = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
 
 
-def group_columns_layout(shape, moved_axes):
+def group_columns_layout(shape, moved_axes, itemsize=8):
     """(outer, m, inner) when the reduced axes are consecutive, increasing and not last
     (a C-contiguous array is then `outer` blocks of m x `inner` values, the labels
-    running over m) and there are enough columns for the column kernel; else None."""
+    running over m) and there are enough columns for the column kernel to beat the copy
+    (`_host.column_min`); else None."""
     if not moved_axes:
         return None
     axes = tuple(moved_axes)
@@ -172,7 +173,7 @@ def group_columns_layout(shape, moved_axes):
     outer = math.prod(shape[:k0])
     m = math.prod(shape[k0 : axes[-1] + 1])
     inner = math.prod(shape[axes[-1] + 1 :])
-    if outer * inner < _host.MIN_COLUMNS:
+    if outer * inner < _host.column_min(itemsize):
         return None
     return outer, m, inner
 
@@ -183,7 +184,7 @@ def _group_columns(name, v, lab, moved_axes, num_labels, ddof):
     results bit for bit).  None when that does not apply."""
     if v.dtype not in _COLS_DTYPES or not v.is_contiguous():
         return None
-    layout = group_columns_layout(tuple(v.shape), moved_axes)
+    layout = group_columns_layout(tuple(v.shape), moved_axes, v.element_size())
     if layout is None:
         return None
     L = _lib.lib()

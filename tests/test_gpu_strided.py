@@ -1,12 +1,14 @@
 """A scanned axis that is not the last one (numbagg's gufuncs take such strided core
 axes directly, numbagg/decorators.py:340-341, :409-414, :480-487).
 
-For C-contiguous arrays with enough columns the fills, the moving windows and the
-exponentially weighted family run one thread per column, in place, instead of moving
-the axis last and copying.  That kernel repeats numbagg's loop operation for operation, so float64 (and
+For C-contiguous arrays with enough columns (256 KB of them per position, where the
+in-place kernel beats moving the axis last with a copy) the fills, the moving windows,
+the exponentially weighted family and the grouped reductions run one thread per column,
+in place.  That kernel repeats numbagg's loop operation for operation, so float64 (and
 float32 with a float32 alpha) results must equal the oracle bit for bit; the
-FP32-compensated form keeps its stated 2e-6.  The last tests make the calls that
-xarray's rolling_exp and flox's grouped reductions make.
+FP32-compensated form keeps its stated 2e-6.  Narrower arrays take the copy and the row
+kernels.  The last tests make the calls that xarray's rolling_exp and flox's grouped
+reductions make.
 """
 
 import numpy as np
@@ -31,7 +33,11 @@ def _data(shape, seed, p_nan=0.1, dtype=np.float64):
     return x.astype(dtype)
 
 
-@pytest.mark.parametrize("shape,axis", [((3000, 4096), 0), ((5, 2000, 600), 1), ((400, 3, 2048), 0)])
+# The first three are wide enough for the in-place column kernel (for 4-byte values
+# too); the last two take the copy and the row kernel (the fills are exact either way)
+@pytest.mark.parametrize("shape,axis", [
+    ((200, 65536), 0), ((5, 300, 13200), 1), ((120, 3, 22000), 0), ((3000, 4096), 0), ((5, 2000, 600), 1),
+])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32])
 @pytest.mark.parametrize("fname", ["ffill", "bfill"])
 def test_fill_non_last_axis(fname, dtype, shape, axis):
@@ -40,7 +46,8 @@ def test_fill_non_last_axis(fname, dtype, shape, axis):
         x = x.astype(dtype)
         x[(np.random.default_rng(32).random(shape) < 0.3)] = np.nan  # runs of missing values
     xt = torch.from_numpy(np.ascontiguousarray(x)).cuda()
-    assert _host.column_layout(xt, axis) is not None  # the in-place column path
+    cols = int(np.prod(shape)) // shape[axis]
+    assert (_host.column_layout(xt, axis) is not None) == (cols >= _host.column_min(x.itemsize))
     for limit in (None, 3):
         got = getattr(nb, fname)(xt, limit=limit, axis=axis).cpu().numpy()
         want = oracle.fill(fname, x, limit=limit, axis=axis)
@@ -52,7 +59,7 @@ MOVE = ["move_sum", "move_mean", "move_var", "move_std", "move_cov", "move_corr"
 
 @pytest.mark.parametrize("fname", MOVE)
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("shape,axis", [((1500, 2500), 0), ((4, 700, 1024), 1)])
+@pytest.mark.parametrize("shape,axis", [((320, 65536), 0), ((2, 400, 32768), 1)])
 def test_move_non_last_axis_bit_exact(fname, dtype, shape, axis):
     x = _data(shape, 41, dtype=dtype)
     y = _data(shape, 42, dtype=dtype) if fname in ("move_cov", "move_corr") else None
@@ -80,7 +87,7 @@ def test_move_non_last_axis_fp32c_keeps_its_bound():
 @pytest.mark.parametrize("fname", MOVE_EXP)
 @pytest.mark.parametrize("alpha_kind", ["scalar", "1d", "nd"])
 def test_move_exp_non_last_axis_bit_exact(fname, alpha_kind):
-    shape, axis = (1500, 2500), 0
+    shape, axis = (300, 32768), 0
     x = _data(shape, 33)
     y = _data(shape, 34) if fname in ("move_exp_nancov", "move_exp_nancorr") else None
     rng = np.random.default_rng(35)
@@ -99,7 +106,7 @@ def test_move_exp_non_last_axis_bit_exact(fname, alpha_kind):
 
 @pytest.mark.parametrize("fname", ["move_exp_nanmean", "move_exp_nanvar", "move_exp_nancorr"])
 def test_move_exp_non_last_axis_float32_and_fp32c(fname):
-    shape, axis = (1200, 3000), 0
+    shape, axis = (200, 65536), 0  # float32 needs 65,536 columns for the in-place kernel
     x = _data(shape, 36)
     y = _data(shape, 37) if fname == "move_exp_nancorr" else None
     func = getattr(nb, fname)
@@ -134,7 +141,7 @@ def test_xarray_style_calls():
     # xarray's rolling_exp calls numbagg.move_exp_nanmean / nansum(array, axis=..., alpha=...,
     # min_weight=...) with the time axis anywhere; its ffill / bfill pass limit and axis
     rng = np.random.default_rng(39)
-    da = rng.standard_normal((365, 40, 80))  # time, lat, lon
+    da = rng.standard_normal((365, 128, 256))  # time, lat, lon: 32,768 columns, in place
     da[rng.random(da.shape) < 0.05] = np.nan
     for f in ("move_exp_nanmean", "move_exp_nansum", "move_exp_nanstd"):
         got = getattr(nb, f)(da, axis=0, alpha=0.2, min_weight=0.5)
@@ -176,7 +183,8 @@ def test_group_non_last_axes_bit_exact(fname, dtype):
     # numbagg's loop in place, so every function's results are the reference's bit for
     # bit (float sums rounded per addition, integer sums and products wrapping)
     rng = np.random.default_rng(44)
-    cases = [((700, 4096), 0, 12), ((3, 40, 50, 2100), (1, 2), 7), ((5, 300, 2048), 1, 30)]
+    c = _host.column_min(np.dtype(dtype).itemsize)  # columns for the in-place kernel
+    cases = [((64, c), 0, 12), ((2, 8, 4, c // 2), (1, 2), 7), ((2, 50, c // 2), 1, 30)]
     for shape, axis, K in cases:
         if np.issubdtype(dtype, np.floating):
             x = (rng.standard_normal(shape) * 3 + 1).astype(dtype)
@@ -191,6 +199,7 @@ def test_group_non_last_axes_bit_exact(fname, dtype):
         labels = rng.integers(-1, K + 2, size=lshape)  # negative and >= num_labels skipped
         xt = torch.from_numpy(x).cuda()
         lt = torch.from_numpy(labels).cuda()
+        assert nb.grouped.group_columns_layout(shape, ax, x.itemsize) is not None
         kw = {"ddof": 0} if fname in ("group_nanvar", "group_nanstd") else {}
         got = getattr(nb, fname)(xt, lt, axis=axis, num_labels=K, **kw).cpu().numpy()
         want = oracle.group(fname, x, labels, axis=axis, num_labels=K, **kw)

@@ -136,12 +136,17 @@ def test_in_place_layouts():
     from numbagg_gb300.aggregate import middle_inner
 
     # scans: a non-last axis of a C-contiguous array with enough columns
-    t = torch.empty((100, 4096))
-    assert _host.column_layout(t, 0) == (1, 100, 4096)
+    t = torch.empty((100, 32768), dtype=torch.float64)
+    assert _host.column_layout(t, 0) == (1, 100, 32768)
     assert _host.column_layout(t, 1) is None  # the last axis: the rows kernels
-    assert _host.column_layout(torch.empty((3, 50, 1000)), 1) == (3, 50, 1000)
+    assert _host.column_layout(torch.empty((3, 50, 11000), dtype=torch.float64), 1) == (3, 50, 11000)
     assert _host.column_layout(torch.empty((100, 7)), 0) is None  # too few columns
     assert _host.column_layout(torch.empty((4096, 100)).T, 0) is None  # not contiguous
+    # the in-place kernels need 256 KB of columns per position to beat the copy
+    assert _host.column_min(8) == 32768 and _host.column_min(4) == 65536
+    assert _host.column_layout(torch.empty((100, 16384), dtype=torch.float64), 0) is None
+    assert _host.column_layout(torch.empty((100, 32768), dtype=torch.float32), 0) is None
+    assert _host.column_layout(torch.empty((100, 16384), dtype=torch.float64), 0, 2048) == (1, 100, 16384)
     # static aggregations: consecutive middle axes, increasing, not last
     assert middle_inner((4, 40, 50, 64), (1, 2)) == 64
     assert middle_inner((4, 40, 50, 64), (0,)) == 40 * 50 * 64
@@ -153,10 +158,11 @@ def test_in_place_layouts():
     # grouped reductions: consecutive increasing reduced axes, not the last one
     from numbagg_gb300.grouped import group_columns_layout
 
-    assert group_columns_layout((700, 4096), (0,)) == (1, 700, 4096)
-    assert group_columns_layout((3, 40, 50, 2100), (1, 2)) == (3, 2000, 2100)
-    assert group_columns_layout((3, 40, 50, 2100), (2, 1)) is None  # the labels' order would change
-    assert group_columns_layout((3, 40, 50, 2100), (2, 3)) is None  # includes the last axis
-    assert group_columns_layout((3, 40, 50, 2100), (0, 2)) is None  # not consecutive
-    assert group_columns_layout((700, 8), (0,)) is None  # too few columns
-    assert group_columns_layout((700, 4096), None) is None  # labels over every axis
+    assert group_columns_layout((700, 32768), (0,)) == (1, 700, 32768)
+    assert group_columns_layout((3, 40, 50, 11000), (1, 2)) == (3, 2000, 11000)
+    assert group_columns_layout((3, 40, 50, 11000), (2, 1)) is None  # the labels' order would change
+    assert group_columns_layout((3, 40, 50, 11000), (2, 3)) is None  # includes the last axis
+    assert group_columns_layout((3, 40, 50, 11000), (0, 2)) is None  # not consecutive
+    assert group_columns_layout((700, 4096), (0,)) is None  # too few columns to beat the copy
+    assert group_columns_layout((700, 32768), (0,), itemsize=4) is None  # float32 needs twice as many
+    assert group_columns_layout((700, 32768), None) is None  # labels over every axis
