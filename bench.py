@@ -63,11 +63,12 @@ def parse_args(argv=None):
     p.add_argument("--only", default=None, help="regex: time only the calls whose key matches (profiling)")
     p.add_argument(
         "--suite",
-        choices=("group_fill", "scan", "ragged", "link", "aggregate"),
+        choices=("group_fill", "scan", "ragged", "link", "aggregate", "columns"),
         default="group_fill",
         help="group_fill: the headline workload; scan: the moving-window, EWM and matrix shapes; "
         "ragged: the batched mix of series of uneven length; link: pinned host<->device copy "
-        "bandwidth (the bound of the end-to-end number); aggregate: the static aggregations",
+        "bandwidth (the bound of the end-to-end number); aggregate: the static aggregations; "
+        "columns: a non-last axis in place against moving it last with a copy",
     )
     p.add_argument("--ragged-series", type=int, default=100_000, help="series in the ragged batch")
     p.add_argument(
@@ -1183,6 +1184,73 @@ def run_link_suite(args):
     return 0
 
 
+def run_columns_suite(args):
+    """Along axis 0 of float64 arrays (1 GiB, 5% NaN): each family through the public
+    API, where the library chooses (`chosen`), forced in place through its column kernel
+    (`in_place`), and with the axis moved last by a copy before the row kernel
+    (`moved`).  The library's crossover between the two comes from this measurement."""
+    import torch
+
+    import numbagg_gb300 as nb
+    from numbagg_gb300 import _host
+
+    world, rank, local = dist_env()
+    device = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(device)
+    stream = torch.cuda.current_stream(device)
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        return round(e0.elapsed_time(e1) / args.steps, 3)
+
+    res = {}
+    for shape in ((16384, 8192), (2048, 65536)):
+        g = torch.Generator(device=device)
+        g.manual_seed(0)
+        x = torch.randn(shape, generator=g, dtype=torch.float64, device=device)
+        x[torch.rand(shape, generator=g, device=device) < NAN_P] = float("nan")
+        lab = torch.randint(0, 12, (shape[0],), generator=g, device=device, dtype=torch.int32)
+        families = {
+            "ffill": lambda v, ax: nb.ffill(v, axis=ax),
+            "move_mean_w20": lambda v, ax: nb.move_mean(v, window=20, axis=ax),
+            "move_exp_nanmean_a0.1": lambda v, ax: nb.move_exp_nanmean(v, alpha=0.1, axis=ax),
+            "group_nansum_K12": lambda v, ax: nb.group_nansum(v, lab, axis=ax, num_labels=12),
+            "group_nanargmax_K12": lambda v, ax: nb.group_nanargmax(v, lab, axis=ax, num_labels=12),
+        }
+        for name, f in families.items():
+            chosen = timed(lambda: f(x, 0))
+            saved = _host.COLUMN_MIN_ROW_BYTES
+            _host.COLUMN_MIN_ROW_BYTES = 0  # the column kernel whatever the width
+            try:
+                in_place = timed(lambda: f(x, 0))
+            finally:
+                _host.COLUMN_MIN_ROW_BYTES = saved
+            moved = timed(lambda: f(x.T.contiguous(), -1))
+            res[f"{name} {shape[0]}x{shape[1]}"] = {"chosen_ms": chosen, "in_place_ms": in_place, "moved_ms": moved}
+        del x
+        torch.cuda.empty_cache()
+    line = {
+        "suite": "columns",
+        "metric": "ms per call along axis 0: the library's choice, the in-place column kernel, the copy + row kernel",
+        "config": {"values": f"float64, N(0,1), {NAN_P:.0%} NaN, 1 GiB per array", "labels": "int32 U[0, 12) along axis 0",
+                   "crossover": f"in place from {_host.COLUMN_MIN_ROW_BYTES} bytes of columns per position"},
+        "per_call": res,
+        "steps": args.steps,
+        "warmup": args.warmup,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -1195,6 +1263,8 @@ def main(argv=None):
         return run_link_suite(args)
     if args.suite == "aggregate":
         return run_aggregate_suite(args)
+    if args.suite == "columns":
+        return run_columns_suite(args)
     return run_ours(args)
 
 
