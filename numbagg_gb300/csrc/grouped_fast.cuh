@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(FT) mid_mom_kernel(const V* __restrict__ value
 }
 
 template <int F, typename V, typename L>
-__global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
+__global__ void __launch_bounds__(FT, 3) mid_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                      long long rows, long long m, int K, long long chunk_len,
                                                      long long chunks, SelPart* __restrict__ parts) {
   typedef typename BitsOf<V>::type B;
@@ -741,17 +741,28 @@ __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ value
   }
   __syncthreads();
   const B* vr = as_bits(values) + row * m;
-  for (long long base = c0; base < c1; base += kCtaCols) {
-    B v[8];
-    int lab[8];
+  // the next tile's loads are issued before the current tile updates the bins, so a
+  // tile is always in flight
+  auto load = [&](long long base, B (&v)[8], int (&lab)[8]) {
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const long long col = base + j * FT + tid;
       const bool in = col < c1;
       v[j] = in ? __ldcs(vr + col) : B(0);
       const long long l = in ? static_cast<long long>(__ldg(labels + col)) : -1;
-      lab[j] = (l >= 0 && l < K && !nan_bits(v[j])) ? static_cast<int>(l) : -1;
+      lab[j] = (l >= 0 && l < K) ? static_cast<int>(l) : -1;
     }
+  };
+  B v[8];
+  int lab[8];
+  load(c0, v, lab);
+  for (long long base = c0; base < c1; base += kCtaCols) {
+    B vn[8];
+    int ln[8];
+    load(base + kCtaCols, vn, ln);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (nan_bits(v[j])) lab[j] = -1;
     // Every lane runs the whole update (its loads, then a compare-and-swap loop that
     // rarely iterates): measured several times faster here than first filtering on
     // the bin's key, which makes the warp diverge around the loop.
@@ -767,6 +778,11 @@ __global__ void __launch_bounds__(FT) mid_sel_kernel(const V* __restrict__ value
       } else {
         sel_update(b, sel_key_of<F>(v[j]), c, true);
       }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      v[j] = vn[j];
+      lab[j] = ln[j];
     }
   }
   __syncthreads();
