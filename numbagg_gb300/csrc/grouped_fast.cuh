@@ -982,7 +982,16 @@ __global__ void __launch_bounds__(FT, 2) big_var_kernel(const V* __restrict__ va
 // data again and reduces the column with min wherever an element's key equals its
 // bin's maximum -- the first column holding the maximum, as the reference's strict
 // comparison keeps.  Exact and independent of the order of the reductions.
-template <int F, typename V, typename L, int RB, int PASS>
+//
+// HL (float64 values, fewer than 2^32 - 1 columns): the L2 serves these reductions and
+// loads by 32-byte sectors, so pass 0 reduces only the high 32 bits of each key (eight
+// rows' words per sector instead of four) and pass 1 loads those; an element whose high
+// half equals its bin's is a candidate and reduces (low 32 bits of its key, 2^32 - 1 -
+// column) with max into a 64-bit word.  Every element holding the maximum key is a
+// candidate, and among candidates (same high half) the low half orders the keys, so the
+// word ends with the maximum key's first column: the same result with half the sector
+// operations.
+template <int F, typename V, typename L, int RB, int PASS, bool HL>
 __global__ void __launch_bounds__(FT, 2) big_sel_kernel(const V* __restrict__ values, const L* __restrict__ labels,
                                                         long long rows, long long m, long long K, long long chunk_len,
                                                         long long chunks, unsigned long long* __restrict__ kmax,
@@ -995,6 +1004,7 @@ __global__ void __launch_bounds__(FT, 2) big_sel_kernel(const V* __restrict__ va
   const bool live = rb * RB + r < rows;
   const long long off = rb * K * RB + r;
   const unsigned long long keep = l2_evict_last();
+  unsigned* khi = reinterpret_cast<unsigned*>(kmax);  // HL: high halves, 4 bytes a bin
   big_tiles<V, L, RB>(values, labels, rows, m, rb, c0, c1, st,
                       [&](const B (&ev)[kBigT], const int (&el)[kBigT], long long cbase) {
                         if (PASS == 0) {
@@ -1006,7 +1016,26 @@ __global__ void __launch_bounds__(FT, 2) big_sel_kernel(const V* __restrict__ va
                             const unsigned long long c = static_cast<unsigned long long>(big_col<RB>(cbase, e));
                             if (F == kFirst) red_min_hint(&imin[a], c, keep);
                             else if (F == kLast) red_max_hint(&kmax[a], c + 1, keep);
+                            else if (HL) red_max_hint(&khi[a], static_cast<unsigned>(sel_key_of<F>(ev[e]) >> 32), keep);
                             else red_max_hint(&kmax[a], sel_key_of<F>(ev[e]), keep);
+                          }
+                        } else if (HL) {
+                          unsigned best[kBigT];  // independent loads, all in flight
+#pragma unroll
+                          for (int e = 0; e < kBigT; ++e) {
+                            const int l = el[e];
+                            best[e] = 0u;
+                            if (live && l >= 0 && l < K) best[e] = ld_keep(&khi[off + static_cast<long long>(l) * RB], keep);
+                          }
+#pragma unroll
+                          for (int e = 0; e < kBigT; ++e) {
+                            const int l = el[e];
+                            if (!live || l < 0 || l >= K || nan_bits(ev[e])) continue;
+                            const unsigned long long key = sel_key_of<F>(ev[e]);
+                            if (static_cast<unsigned>(key >> 32) != best[e]) continue;
+                            const unsigned long long c = static_cast<unsigned long long>(big_col<RB>(cbase, e));
+                            red_max_hint(&imin[off + static_cast<long long>(l) * RB], (key << 32) | (0xffffffffull - c),
+                                         keep);
                           }
                         } else {
                           unsigned long long best[kBigT];  // independent loads, all in flight
@@ -1233,7 +1262,7 @@ NBG_DEVICE O finish_sel(unsigned long long key, unsigned long long idx, const V*
   return static_cast<O>(static_cast<double>(vrow[idx]));  // max / min via the float64 running value
 }
 
-template <int F, typename V, typename O, int RB>
+template <int F, typename V, typename O, int RB, bool HL>
 __global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ kmax,
                                       const unsigned long long* __restrict__ imin, const V* __restrict__ values,
                                       O* __restrict__ out, long long rows, long long m, long long K) {
@@ -1244,8 +1273,14 @@ __global__ void big_sel_finish_kernel(const unsigned long long* __restrict__ kma
     const long long k = rem / RB, row = rb * RB + (rem - k * RB);
     if (row >= rows) continue;
     // finish_sel's (key, index) convention: first keeps its column in the key
-    const unsigned long long key = F == kFirst ? imin[t] : kmax[t];
-    const unsigned long long idx = (F == kFirst || F == kLast) ? 0ull : (kmax[t] ? imin[t] : ~0ull);
+    unsigned long long key, idx;
+    if (HL) {  // (low half of the key, 2^32 - 1 - column); 0: no element
+      key = imin[t];
+      idx = key ? 0xffffffffull - (key & 0xffffffffull) : ~0ull;
+    } else {
+      key = F == kFirst ? imin[t] : kmax[t];
+      idx = (F == kFirst || F == kLast) ? 0ull : (kmax[t] ? imin[t] : ~0ull);
+    }
     out[row * K + k] = finish_sel<F, V, O>(key, idx, values + row * m);
   }
 }
@@ -1286,7 +1321,9 @@ struct FastPlan {
 // accumulators (K x RB x the bytes a bin keeps) stay within 64 MB of the L2, and no
 // more than the rows rounded up to a power of two.
 inline int big_rows_per_block(int f, long long rows, long long K) {
-  size_t per = 16;  // selection: (key, index)
+  // selection: the bins that pass 0 reduces (8-byte keys; the float64 argmax / argmin /
+  // max / min reduce 4-byte high halves there, so rows per block double for them)
+  size_t per = 8;
   if (is_moments(f)) {
     per = 4;  // NaN count (count / mean / var / std; kept for the others too)
     if (f == kSum || f == kMean || f == kVar || f == kStd) per += 8;
@@ -1430,16 +1467,29 @@ int launch_big_sel(const V* values, const L* labels, O* out, long long rows, lon
   const long long slots = p.blocks * RB * K;
   unsigned long long* kmax = carve<unsigned long long>(cur, slots);
   unsigned long long* imin = carve<unsigned long long>(cur, slots);
+  const int grid = static_cast<int>(p.blocks * p.chunks);
+  constexpr bool kHLType = sizeof(V) == 8 && IsFloat<V>::value && F != kFirst && F != kLast;
+  if (kHLType && m < 0xffffffffll) {
+    cudaMemsetAsync(kmax, 0, static_cast<size_t>(slots) * 4, s);  // high halves: none yet
+    cudaMemsetAsync(imin, 0, static_cast<size_t>(slots) * 8, s);  // no candidate yet
+    big_sel_kernel<F, V, L, RB, 0, kHLType><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks,
+                                                                 kmax, imin);
+    big_sel_kernel<F, V, L, RB, 1, kHLType><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks,
+                                                                 kmax, imin);
+    big_sel_finish_kernel<F, V, O, RB, kHLType><<<fin_grid(slots), 256, 0, s>>>(kmax, imin, values, out, rows, m, K);
+    return 3;
+  }
   cudaMemsetAsync(kmax, 0, static_cast<size_t>(slots) * 8, s);     // below every key and column + 1
   cudaMemsetAsync(imin, 0xff, static_cast<size_t>(slots) * 8, s);  // no column yet
-  const int grid = static_cast<int>(p.blocks * p.chunks);
-  big_sel_kernel<F, V, L, RB, 0><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax, imin);
+  big_sel_kernel<F, V, L, RB, 0, false><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax,
+                                                              imin);
   int launches = 1;
   if (F != kFirst && F != kLast) {
-    big_sel_kernel<F, V, L, RB, 1><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax, imin);
+    big_sel_kernel<F, V, L, RB, 1, false><<<grid, FT, 0, s>>>(values, labels, rows, m, K, p.chunk_len, p.chunks, kmax,
+                                                                imin);
     ++launches;
   }
-  big_sel_finish_kernel<F, V, O, RB><<<fin_grid(slots), 256, 0, s>>>(kmax, imin, values, out, rows, m, K);
+  big_sel_finish_kernel<F, V, O, RB, false><<<fin_grid(slots), 256, 0, s>>>(kmax, imin, values, out, rows, m, K);
   return launches + 1;
 }
 

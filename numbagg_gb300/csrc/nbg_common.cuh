@@ -102,6 +102,14 @@ NBG_DEVICE unsigned long long ld_keep(const unsigned long long* a, unsigned long
 NBG_DEVICE void red_add_hint(unsigned* a, unsigned v, unsigned long long pol) {
   asm volatile("red.global.add.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
 }
+NBG_DEVICE void red_max_hint(unsigned* a, unsigned v, unsigned long long pol) {
+  asm volatile("red.global.max.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+}
+NBG_DEVICE unsigned ld_keep(const unsigned* a, unsigned long long pol) {
+  unsigned v;
+  asm volatile("ld.global.cg.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
 
 // Ask L2 for a line ahead of its use (no register, no fault on a valid address); the
 // column kernels walk a column serially, so this is their memory-level parallelism.
